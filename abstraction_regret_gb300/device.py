@@ -1,0 +1,168 @@
+"""Device-resident automata: the engine's GPU layouts, built once per automaton.
+
+The reference re-uploads the CSR and re-packs the accept words on every call
+(src/gpufsm/backends/cuda/nfa.py:44-52 and :105-121, ``dev_copy`` in
+native/include/common.cuh:150-159). Here an automaton is uploaded once, converted on the
+device by the layout kernels of ``libgbfsm`` (which also validate every index), and kept
+resident as PyTorch tensors for as long as its executor lives.
+
+NFA layout (``gbfsm_nfa_dev``): uint32 row arrays, 16-byte edge records
+``{target, symbol | accept/eps flags of target, target's edge-row begin, end}`` and the
+packed accept words (pack_accept layout). DFA layout (``gbfsm_dfa_dev``): 2-byte entries
+(up to 32768 states) or 4-byte entries holding the successor with ``accept[successor]``
+in the top bit, plus packed accept bits.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import native
+from .automata import ALPHABET, ANY_SYMBOL
+from .packing import words_for
+
+
+def _stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _padded(n_elems: int, elem_bytes: int, device, dtype=torch.uint8) -> torch.Tensor:
+    """A zero-filled device buffer of at least ``n_elems * elem_bytes`` bytes, padded to 16."""
+    nbytes = max(16, -(-(n_elems * elem_bytes) // 16) * 16)
+    itemsize = torch.empty((), dtype=dtype).element_size()
+    return torch.zeros(nbytes // itemsize, dtype=dtype, device=device)
+
+
+def _to_dev(a: np.ndarray, dtype, device) -> torch.Tensor:
+    arr = np.ascontiguousarray(a, dtype=dtype)
+    if arr.size == 0:
+        arr = np.zeros(4, dtype=dtype)
+    return torch.from_numpy(arr).to(device)
+
+
+def resolve_device(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("the CUDA backend needs a CUDA device (torch.cuda.is_available() is False)")
+    if device is None:
+        return torch.device("cuda", torch.cuda.current_device())
+    d = torch.device(device)
+    if d.type != "cuda":
+        raise ValueError(f"device must be a CUDA device, got {d}")
+    return torch.device("cuda", d.index if d.index is not None else torch.cuda.current_device())
+
+
+class DeviceNFA:
+    """An NFA (ours or gpufsm's, duck-typed on the CSR fields) resident on a GPU."""
+
+    def __init__(self, nfa, device=None) -> None:
+        dev = resolve_device(device)
+        lib = native.lib()
+        n = int(nfa.num_states)
+        if n < 1:
+            raise ValueError("cannot simulate an NFA with zero states")
+        start = int(nfa.start_state)
+        if not 0 <= start < n:
+            raise ValueError(f"start_state {start} out of range (0..{n - 1})")
+        srp = np.asarray(nfa.sym_row_ptr)
+        erp = np.asarray(nfa.eps_row_ptr)
+        if srp.shape != (n + 1,) or erp.shape != (n + 1,):
+            raise ValueError("row pointer arrays must have num_states + 1 entries")
+        ssy = np.asarray(nfa.sym_symbols)
+        nnz, nne = int(srp[-1]), int(erp[-1])
+        if nnz != np.asarray(nfa.sym_targets).size or nne != np.asarray(nfa.eps_targets).size:
+            raise ValueError("row pointers disagree with the edge array lengths")
+        self.device = dev
+        self.num_states = n
+        self.start_state = start
+        self.num_words = words_for(n)
+        self.num_sym_edges = nnz
+        self.num_eps_edges = nne
+        self.has_eps = nne > 0
+        self.uses_any = bool(np.any(ssy == ANY_SYMBOL)) if nnz else False
+        with torch.cuda.device(dev):
+            src = [_to_dev(nfa.sym_row_ptr, np.int32, dev), _to_dev(nfa.sym_targets, np.int32, dev),
+                   _to_dev(nfa.sym_symbols, np.int32, dev), _to_dev(nfa.eps_row_ptr, np.int32, dev),
+                   _to_dev(nfa.eps_targets, np.int32, dev), _to_dev(nfa.accept, np.uint8, dev)]
+            self.sym_row = _padded(n + 1, 4, dev)
+            self.eps_row = _padded(n + 1, 4, dev)
+            self.sym_edges = _padded(max(nnz, 1), 16, dev)
+            self.eps_edges = _padded(max(nne, 1), 16, dev)
+            self.accept_words = _padded(self.num_words, 8, dev)
+            err = torch.zeros(4, dtype=torch.int32, device=dev)
+            status = lib.gbfsm_nfa_layout(
+                n, src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), src[3].data_ptr(),
+                src[4].data_ptr(), src[5].data_ptr(), nnz, nne, self.sym_row.data_ptr(),
+                self.sym_edges.data_ptr(), self.eps_row.data_ptr(), self.eps_edges.data_ptr(),
+                self.accept_words.data_ptr(), err.data_ptr(), _stream_handle(dev))
+            native.check(status, "gbfsm_nfa_layout")
+            code = int(err[0].item())  # synchronises: the layout is checked before any use
+            if code:
+                raise ValueError(f"invalid NFA: layout check failed with code {code} "
+                                 f"(1 row pointers, 2 target, 3 symbol, 4 epsilon target)")
+        d = native.NfaDev()
+        d.num_states = n
+        d.start_state = start
+        d.num_words = self.num_words
+        d.flags = (native.NFA_HAS_EPS if self.has_eps else 0) | (
+            native.NFA_HAS_ANY if self.uses_any else 0)
+        d.sym_row = self.sym_row.data_ptr()
+        d.sym_edges = self.sym_edges.data_ptr()
+        d.eps_row = self.eps_row.data_ptr()
+        d.eps_edges = self.eps_edges.data_ptr()
+        d.accept_words = self.accept_words.data_ptr()
+        d.num_sym_edges = nnz
+        d.num_eps_edges = nne
+        self.desc = d
+
+    @property
+    def edge_bytes(self) -> int:
+        """Bytes of the resident layout (rows + edge records + accept words)."""
+        return (self.sym_row.numel() + self.eps_row.numel() + self.sym_edges.numel()
+                + self.eps_edges.numel() + self.accept_words.numel())
+
+
+class DeviceDFA:
+    """A DFA (ours or gpufsm's) resident on a GPU as a packed transition table."""
+
+    def __init__(self, dfa, device=None, entry_bytes: int | None = None) -> None:
+        dev = resolve_device(device)
+        lib = native.lib()
+        n = int(dfa.num_states)
+        if n < 1:
+            raise ValueError("cannot simulate a DFA with zero states")
+        start = int(dfa.start_state)
+        if not 0 <= start < n:
+            raise ValueError(f"start_state {start} out of range (0..{n - 1})")
+        trans = np.asarray(dfa.trans)
+        if trans.size != n * ALPHABET:
+            raise ValueError(f"trans must have num_states * 256 = {n * ALPHABET} entries")
+        if entry_bytes is None:
+            entry_bytes = 2 if n <= 32768 else 4
+        self.device = dev
+        self.num_states = n
+        self.start_state = start
+        self.entry_bytes = entry_bytes
+        self.table_bytes = n * ALPHABET * entry_bytes
+        with torch.cuda.device(dev):
+            t_dev = _to_dev(trans, np.int32, dev)
+            a_dev = _to_dev(dfa.accept, np.uint8, dev)
+            self.table = _padded(n * ALPHABET, entry_bytes, dev)
+            self.accept_bits = _padded(-(-n // 32), 4, dev)
+            err = torch.zeros(4, dtype=torch.int32, device=dev)
+            status = lib.gbfsm_dfa_layout(n, t_dev.data_ptr(), a_dev.data_ptr(), entry_bytes,
+                                          self.table.data_ptr(), self.accept_bits.data_ptr(),
+                                          err.data_ptr(), _stream_handle(dev))
+            native.check(status, "gbfsm_dfa_layout")
+            code = int(err[0].item())
+            if code:
+                raise ValueError(f"invalid DFA: a successor is outside [0, {n}) (code {code})")
+        d = native.DfaDev()
+        d.num_states = n
+        d.start_state = start
+        d.entry_bytes = entry_bytes
+        d.flags = 0
+        d.table = self.table.data_ptr()
+        d.accept_bits = self.accept_bits.data_ptr()
+        d.table_bytes = self.table_bytes
+        self.desc = d

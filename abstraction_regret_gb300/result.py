@@ -1,0 +1,94 @@
+"""Result and benchmark-statistics types (reference: ``src/gpufsm/core/result.py:11-94``).
+
+Same fields, same equality rule (``matches`` compares the verdict only) and the same
+batch timing convention: a batched launch has one kernel time, reported on the first
+result of the batch, with zeros on the rest, so ``results[0].kernel_ms`` is always the
+batch time.
+"""
+
+from __future__ import annotations
+
+import math
+from collections.abc import Sequence
+from dataclasses import dataclass, field
+from typing import Any
+
+
+@dataclass
+class Result:
+    """Verdict and timings of one input on one backend/technique."""
+
+    accepted: bool
+    match_len: int
+    kernel_ms: float = 0.0
+    total_ms: float = 0.0
+    transfer_ms: float = 0.0
+    mem_bytes: int = 0
+
+    def matches(self, other: Result) -> bool:
+        """True when both verdicts agree; timings are not compared."""
+        return self.accepted == other.accepted and self.match_len == other.match_len
+
+
+def batch_results(
+    flags: Sequence[Any],
+    lens: Sequence[Any],
+    kernel_ms: float,
+    transfer_ms: float = 0.0,
+) -> list[Result]:
+    """One :class:`Result` per input, with the batch's times on the first one only."""
+    out = []
+    for i in range(len(flags)):
+        first = i == 0
+        out.append(
+            Result(
+                accepted=bool(flags[i]),
+                match_len=int(lens[i]),
+                kernel_ms=kernel_ms if first else 0.0,
+                total_ms=(kernel_ms + transfer_ms) if first else 0.0,
+                transfer_ms=transfer_ms if first else 0.0,
+            )
+        )
+    return out
+
+
+@dataclass
+class BenchmarkStats:
+    """Timings of ``n`` repeated runs after warm-up: mean, sample std, normal CI95."""
+
+    backend: str
+    technique: str
+    accepted: bool
+    match_len: int
+    n: int
+    raw_ms: list[float] = field(default_factory=list)
+
+    @property
+    def mean_ms(self) -> float:
+        return sum(self.raw_ms) / len(self.raw_ms) if self.raw_ms else 0.0
+
+    @property
+    def std_ms(self) -> float:
+        k = len(self.raw_ms)
+        if k < 2:
+            return 0.0
+        m = self.mean_ms
+        return math.sqrt(sum((x - m) ** 2 for x in self.raw_ms) / (k - 1))
+
+    @property
+    def ci95_ms(self) -> float:
+        """Half-width of the normal-approximation 95% interval of the mean."""
+        k = len(self.raw_ms)
+        return 1.96 * self.std_ms / math.sqrt(k) if k >= 2 else 0.0
+
+    def as_row(self) -> dict[str, float | str | int | bool]:
+        return {
+            "backend": self.backend,
+            "technique": self.technique,
+            "accepted": self.accepted,
+            "match_len": self.match_len,
+            "n": self.n,
+            "mean_ms": round(self.mean_ms, 6),
+            "std_ms": round(self.std_ms, 6),
+            "ci95_ms": round(self.ci95_ms, 6),
+        }

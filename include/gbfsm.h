@@ -1,0 +1,312 @@
+/*
+ * gbfsm.h -- C ABI of libgbfsm, the GB300 (sm_103a) automata-simulation engine.
+ *
+ * Drop-in for the native layer of the reference's CUDA backend: gpufsm 0.1.0
+ * (alepot55/abstraction-regret), whose pybind11 module `_cuda` exposes the `run_*`
+ * functions of src/gpufsm/backends/cuda/native/include/api.hpp:23-104 and
+ * bindings.cu:11-39. Two layers are exported:
+ *
+ *  1. Reference-shaped host entry points (gbfsm_run_*): the same arguments and meaning
+ *     as the `_cuda.run_*` functions they replace (host arrays in, host arrays out,
+ *     synchronous, the kernel time in milliseconds), with status codes instead of C++
+ *     exceptions. A ctypes/cffi stub binds them in place of the pybind11 module.
+ *  2. Device entry points (gbfsm_nfa_run, gbfsm_dfa_run, gbfsm_persistent_run, ...):
+ *     device pointers owned by the caller (PyTorch tensors in this package), a CUDA
+ *     stream, no implicit synchronisation, no allocation. These are what the Python
+ *     engine uses; they can be captured in a CUDA graph.
+ *
+ * Conventions for every function:
+ *   - returns gbfsm_status; no exception crosses the ABI; on failure a message is left
+ *     in gbfsm_last_error() (thread-local);
+ *   - `stream` is a cudaStream_t passed as void* (0 = the legacy default stream);
+ *   - verdicts follow the reference's latch-first-match rule (src/gpufsm/reference.py:
+ *     36-81): flags[i] = 1 and lens[i] = the number of bytes consumed when the first
+ *     accepting configuration is reached (0 if the start configuration accepts),
+ *     flags[i] = lens[i] = 0 otherwise;
+ *   - an input is bytes data[offsets[i] .. offsets[i+1]) with int64 offsets. `data`
+ *     must stay readable up to the next 16-byte boundary past offsets[n_inputs] (the
+ *     kernels use 16-byte vector loads); a single input is shorter than 2^31 bytes.
+ */
+#ifndef GBFSM_H
+#define GBFSM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBFSM_ABI_VERSION 1
+#define GBFSM_ANY_SYMBOL 256 /* src/gpufsm/core/nfa.py:16 */
+#define GBFSM_WORD_BITS 64   /* src/gpufsm/core/packing.py:21 */
+
+typedef enum gbfsm_status {
+    GBFSM_OK = 0,
+    GBFSM_INVALID_ARG = 1, /* bad pointer, size or automaton; maps to ValueError */
+    GBFSM_UNSUPPORTED = 2, /* valid but beyond a technique's limits */
+    GBFSM_CUDA_ERROR = 3,  /* a CUDA call failed; maps to RuntimeError */
+    GBFSM_TIMEOUT = 4,     /* a bounded device wait gave up */
+    GBFSM_OOM = 5          /* a host-buffer entry point could not allocate */
+} gbfsm_status;
+
+/* ---------------------------------------------------------------------------------
+ * Device-resident automaton layouts
+ * ------------------------------------------------------------------------------- */
+
+/* One edge of the NFA, 16 bytes. Besides the edge's own target and label it carries
+ * what the simulator needs next about the target (whether it accepts, whether it has
+ * epsilon edges, and the range of its own symbol edges), so following an edge costs
+ * one dependent load instead of three. The same record describes a state in the
+ * engine's active-state lists (target = the state itself). */
+typedef struct gbfsm_edge {
+    uint32_t target;
+    uint32_t info;      /* bits 0-8: symbol (0..255, 256 = ANY); GBFSM_EDGE_* flags */
+    uint32_t row_begin; /* target's symbol edges: sym_edges[row_begin .. row_end) */
+    uint32_t row_end;
+} gbfsm_edge;
+
+#define GBFSM_EDGE_SYMBOL_MASK 0x1FFu
+#define GBFSM_EDGE_ACCEPT (1u << 9)  /* the target accepts */
+#define GBFSM_EDGE_HAS_EPS (1u << 10) /* the target has epsilon edges */
+
+#define GBFSM_NFA_HAS_EPS 1 /* the automaton has epsilon edges */
+#define GBFSM_NFA_HAS_ANY 2 /* the automaton has ANY_SYMBOL edges */
+
+/* An NFA on the device (all pointers are device pointers). Built from the reference's
+ * CSR arrays (src/gpufsm/core/nfa.py:56-65) by gbfsm_nfa_layout. */
+typedef struct gbfsm_nfa_dev {
+    int32_t num_states;
+    int32_t start_state;
+    int32_t num_words; /* ceil(num_states / 64) */
+    int32_t flags;     /* GBFSM_NFA_* */
+    const uint32_t *sym_row;        /* [num_states + 1] */
+    const gbfsm_edge *sym_edges;    /* [num_sym_edges] */
+    const uint32_t *eps_row;        /* [num_states + 1] */
+    const gbfsm_edge *eps_edges;    /* [num_eps_edges] (info symbol bits unused) */
+    const uint64_t *accept_words;   /* [num_words], pack_accept layout */
+    uint64_t num_sym_edges;
+    uint64_t num_eps_edges;
+} gbfsm_nfa_dev;
+
+/* A DFA on the device. table[s * 256 + c] holds the successor of s on byte c in the low
+ * bits and, in the top bit, whether that successor accepts; entries are 2 bytes when
+ * num_states <= 32768, else 4 bytes. accept_bits[s / 32] bit s % 32 = accept[s]. */
+typedef struct gbfsm_dfa_dev {
+    int32_t num_states;
+    int32_t start_state;
+    int32_t entry_bytes; /* 2 or 4 */
+    int32_t flags;
+    const void *table;
+    const uint32_t *accept_bits;
+    uint64_t table_bytes;
+} gbfsm_dfa_dev;
+
+/* How to run a batch. Zero fields select the defaults. */
+typedef struct gbfsm_plan {
+    int32_t technique;     /* GBFSM_TECH_* */
+    int32_t block_threads; /* threads per CTA (multiple of 32) */
+    int32_t list_capacity; /* sparse active-list capacity per warp (COMPACT) */
+    int32_t stage;         /* 1: stage edges / DFA table in shared memory when they fit */
+    int32_t ctas_per_sm;   /* persistent launches: CTAs per SM (0 = from occupancy) */
+    int32_t reserved[3];
+} gbfsm_plan;
+
+#define GBFSM_TECH_BITMAP 0  /* thread per input, packed bitmap set in shared memory */
+#define GBFSM_TECH_WARP 1    /* warp per input, dense bitmap set, ballot/popc/shfl expansion */
+#define GBFSM_TECH_COMPACT 2 /* warp per input, sparse active list; dense when it overflows */
+#define GBFSM_TECH_DFA_WALK 3 /* DFA: thread per input, table walk */
+
+/* ---------------------------------------------------------------------------------
+ * Library
+ * ------------------------------------------------------------------------------- */
+
+/* ABI version of the loaded library (GBFSM_ABI_VERSION). */
+int gbfsm_abi_version(void);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *gbfsm_last_error(void);
+
+/* ---------------------------------------------------------------------------------
+ * Layout builders (device). Replace the per-call host marshalling of
+ * src/gpufsm/backends/cuda/nfa.py:44-52 (_csr_args), :90-100 (pack_accept) and
+ * dfa.py:27-31 with a one-time, device-side build.
+ * ------------------------------------------------------------------------------- */
+
+/* Validate the reference CSR arrays (device pointers, int32 as in core/nfa.py:60-65,
+ * accept as uint8) and write the engine's layout into caller-allocated device arrays:
+ * sym_row/eps_row [n+1], sym_edges [nnz_sym], eps_edges [nnz_eps], accept_words
+ * [ceil(n/64)]. *error (a device int32, zeroed by this call) receives a nonzero code if
+ * an index or symbol is out of range or a row pointer decreases; the caller reads it
+ * after the stream completes. Stream-ordered. */
+gbfsm_status gbfsm_nfa_layout(int32_t num_states, const int32_t *sym_row_ptr,
+                              const int32_t *sym_targets, const int32_t *sym_symbols,
+                              const int32_t *eps_row_ptr, const int32_t *eps_targets,
+                              const uint8_t *accept, uint64_t nnz_sym, uint64_t nnz_eps,
+                              uint32_t *sym_row, gbfsm_edge *sym_edges, uint32_t *eps_row,
+                              gbfsm_edge *eps_edges, uint64_t *accept_words, int32_t *error,
+                              void *stream);
+
+/* Pack the reference DFA table (device int32 [n*256], core/dfa.py:36-41) and accept
+ * array (uint8 [n]) into `table` (entry_bytes per entry) and accept_bits
+ * [ceil(n/32)]. *error as above (a successor out of [0, n)). */
+gbfsm_status gbfsm_dfa_layout(int32_t num_states, const int32_t *trans, const uint8_t *accept,
+                              int32_t entry_bytes, void *table, uint32_t *accept_bits,
+                              int32_t *error, void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * Plain single-launch batch kernels (device pointers). One launch covers the batch.
+ * Replace the kernels behind _cuda.run_worklist / run_worklist_warp /
+ * run_worklist_compact / run_dfa (worklist_register.cu:113-128,
+ * worklist_global.cu:128-181 and :289-310, dfa.cu:9-29).
+ * ------------------------------------------------------------------------------- */
+
+/* Scratch bytes gbfsm_nfa_run needs for `plan` (0 when the sets fit shared memory). */
+size_t gbfsm_nfa_workspace_bytes(const gbfsm_nfa_dev *nfa, int32_t n_inputs,
+                                 const gbfsm_plan *plan);
+
+/* Simulate `nfa` over a batch. examined (nullable) receives the bytes consumed per
+ * input. workspace: device scratch of at least gbfsm_nfa_workspace_bytes. */
+gbfsm_status gbfsm_nfa_run(const gbfsm_nfa_dev *nfa, const uint8_t *data,
+                           const int64_t *offsets, int32_t n_inputs, const gbfsm_plan *plan,
+                           int32_t *flags, int32_t *lens, int32_t *examined, void *workspace,
+                           size_t workspace_bytes, void *stream);
+
+/* Simulate `dfa` over a batch (thread per input; table in shared memory when
+ * plan->stage and it fits, else read through L2). */
+gbfsm_status gbfsm_dfa_run(const gbfsm_dfa_dev *dfa, const uint8_t *data,
+                           const int64_t *offsets, int32_t n_inputs, const gbfsm_plan *plan,
+                           int32_t *flags, int32_t *lens, int32_t *examined, void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * Persistent batched engine (device pointers). Many inputs of uneven length over many
+ * automata of different sizes in ONE launch: resident CTAs pop tasks from a device
+ * queue (one atomic ticket per task) in the order given (the host sorts them longest
+ * first). No counterpart in the reference, which launches once per automaton.
+ * ------------------------------------------------------------------------------- */
+
+/* One entry of the device-resident automaton table. */
+typedef struct gbfsm_automaton {
+    int32_t kind;          /* 0 = NFA, 1 = DFA */
+    int32_t technique;     /* NFA: GBFSM_TECH_WARP or GBFSM_TECH_COMPACT */
+    int32_t list_capacity; /* NFA compact list capacity (<= the launch's capacity) */
+    int32_t reserved;
+    gbfsm_nfa_dev nfa;     /* valid when kind == 0 */
+    gbfsm_dfa_dev dfa;     /* valid when kind == 1 */
+} gbfsm_automaton;
+
+/* One task: `count` inputs of automaton `automaton`, whose input indices are
+ * input_ids[first .. first + count). An NFA task has count 1 (a warp runs it); a DFA
+ * task has 1..32 inputs (one lane each). */
+typedef struct gbfsm_task {
+    int32_t automaton;
+    int32_t first;
+    int32_t count;
+    int32_t reserved;
+} gbfsm_task;
+
+/* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
+size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan);
+
+/* Run `n_tasks` tasks. table/tasks/input_ids are device arrays. Results are written by
+ * input index. workspace (device, >= gbfsm_persistent_workspace_bytes) holds the queue
+ * ticket, which this call resets in-stream, so the launch can be replayed from a graph. */
+gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automata,
+                                  int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
+                                  const int32_t *input_ids, const uint8_t *data,
+                                  const int64_t *offsets, int32_t *flags, int32_t *lens,
+                                  int32_t *examined, void *workspace, size_t workspace_bytes,
+                                  const gbfsm_plan *plan, void *stream);
+
+/* Occupancy query for persistent launches: CTAs of `plan` resident per SM. */
+int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan);
+
+/* ---------------------------------------------------------------------------------
+ * Reference-shaped host entry points: one per `_cuda.run_*` of
+ * src/gpufsm/backends/cuda/native/include/api.hpp:23-104, same argument order and
+ * meaning. Arrays are HOST pointers: the CSR as int32 (nfa.py:44-52), accept words as
+ * uint64 (packing.py:66-85), the batch as int32 symbols with int32 offsets
+ * (packing.py:35-63, num_strings = len(offsets) - 1). Outputs are host arrays of
+ * num_strings int32 and *kernel_ms (device time of the simulation launch). The call is
+ * synchronous on the legacy default stream, like the reference. Each allocates its
+ * device buffers per call and frees them before returning.
+ * ------------------------------------------------------------------------------- */
+
+#define GBFSM_HOST_NFA_BATCH_ARGS                                                          \
+    const int32_t *sym_row_ptr, const int32_t *sym_targets, const int32_t *sym_symbols,    \
+        const int32_t *eps_row_ptr, const int32_t *eps_targets, const uint64_t *accept_words, \
+        const int32_t *input_data, const int32_t *input_offsets, int32_t num_strings,     \
+        int32_t num_states, int32_t start_state, int32_t uses_any, int32_t *out_flags,     \
+        int32_t *out_lens, float *kernel_ms
+
+/* api.hpp:39-44  run_multistream         (bitpacked.cu:233-307)      -> GBFSM_TECH_BITMAP */
+gbfsm_status gbfsm_run_multistream(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:46-51  run_multistream_shared  (bitpacked.cu:310-411)      -> BITMAP, staged edges */
+gbfsm_status gbfsm_run_multistream_shared(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:53-58  run_multistream_async   (bitpacked.cu:420-526)      -> BITMAP, pinned async copies; *kernel_ms is end to end */
+gbfsm_status gbfsm_run_multistream_async(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:62-67  run_worklist            (worklist_register.cu:132-205) -> GBFSM_TECH_BITMAP */
+gbfsm_status gbfsm_run_worklist(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:71-76  run_worklist_global     (worklist_global.cu:347-405) -> GBFSM_TECH_WARP, sets in global scratch */
+gbfsm_status gbfsm_run_worklist_global(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:78-83  run_worklist_warp       (worklist_global.cu:409-468) -> GBFSM_TECH_WARP */
+gbfsm_status gbfsm_run_worklist_warp(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:85-90  run_worklist_compact    (worklist_global.cu:472-528) -> GBFSM_TECH_COMPACT */
+gbfsm_status gbfsm_run_worklist_compact(GBFSM_HOST_NFA_BATCH_ARGS);
+/* api.hpp:92-97  run_worklist_shared     (worklist_global.cu:533-600) -> GBFSM_TECH_WARP, sets in shared memory */
+gbfsm_status gbfsm_run_worklist_shared(GBFSM_HOST_NFA_BATCH_ARGS);
+
+/* api.hpp:23-28 run_dense and api.hpp:32-37 run_bitpacked (one input; dense.cu:66-110,
+ * bitpacked.cu:191-231): (accepted, match_len, kernel_ms) for input_symbols[0..input_len). */
+gbfsm_status gbfsm_run_dense(const int32_t *sym_row_ptr, const int32_t *sym_targets,
+                             const int32_t *sym_symbols, const int32_t *eps_row_ptr,
+                             const int32_t *eps_targets, const int8_t *accept,
+                             const int32_t *input_symbols, int32_t input_len,
+                             int32_t num_states, int32_t start_state, int32_t uses_any,
+                             int32_t *accepted, int32_t *match_len, float *kernel_ms);
+gbfsm_status gbfsm_run_bitpacked(const int32_t *sym_row_ptr, const int32_t *sym_targets,
+                                 const int32_t *sym_symbols, const int32_t *eps_row_ptr,
+                                 const int32_t *eps_targets, const uint64_t *accept_words,
+                                 const int32_t *input_symbols, int32_t input_len,
+                                 int32_t num_states, int32_t start_state, int32_t uses_any,
+                                 int32_t *accepted, int32_t *match_len, float *kernel_ms);
+
+/* api.hpp:101-104 run_dfa (dfa.cu:32-71): trans int32 [num_states*256], accept int8. */
+gbfsm_status gbfsm_run_dfa(const int32_t *trans, const int8_t *accept, const int32_t *input_data,
+                           const int32_t *input_offsets, int32_t num_strings, int32_t num_states,
+                           int32_t start_state, int32_t *out_flags, int32_t *out_lens,
+                           float *kernel_ms);
+
+/* Byte-batch variants of the host path (no counterpart in the reference): uint8 input
+ * bytes and int64 offsets, so 1 byte per symbol crosses the host link instead of 4.
+ * `technique` is a GBFSM_TECH_* value; `plan` may be NULL. */
+gbfsm_status gbfsm_run_nfa_bytes(const int32_t *sym_row_ptr, const int32_t *sym_targets,
+                                 const int32_t *sym_symbols, const int32_t *eps_row_ptr,
+                                 const int32_t *eps_targets, const uint8_t *accept,
+                                 int32_t num_states, int32_t start_state, const uint8_t *data,
+                                 const int64_t *offsets, int32_t num_strings,
+                                 const gbfsm_plan *plan, int32_t *out_flags, int32_t *out_lens,
+                                 float *kernel_ms);
+gbfsm_status gbfsm_run_dfa_bytes(const int32_t *trans, const uint8_t *accept, int32_t num_states,
+                                 int32_t start_state, const uint8_t *data, const int64_t *offsets,
+                                 int32_t num_strings, const gbfsm_plan *plan, int32_t *out_flags,
+                                 int32_t *out_lens, float *kernel_ms);
+
+/* ---------------------------------------------------------------------------------
+ * Synthetic workload generator (host only; no counterpart in the reference, which
+ * draws uniform bytes, src/gpufsm/bench/generators.py:139-161). Writes "live" inputs:
+ * random walks along symbol edges whose targets do not accept and have symbol edges,
+ * so the simulated active set stays non-empty (uniform bytes kill a random NFA within a
+ * byte or two). out[offsets[i] .. offsets[i+1]) receives input i; the bytes depend only
+ * on (automaton, seed, i). Arrays are HOST arrays in the reference CSR layout.
+ * ------------------------------------------------------------------------------- */
+int32_t gbfsm_workload_walk(int32_t num_states, const int32_t *sym_row_ptr,
+                            const int32_t *sym_targets, const int32_t *sym_symbols,
+                            const uint8_t *accept, int32_t start_state, const int64_t *offsets,
+                            int32_t n_inputs, uint64_t seed, uint8_t *out, int32_t n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFSM_H */

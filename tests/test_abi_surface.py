@@ -1,0 +1,111 @@
+"""The C ABI without a GPU: the library loads, exports exactly what include/gbfsm.h
+declares, and rejects bad arguments with status codes (no exception crosses the ABI).
+
+Mirrors the reference's native-surface check (tests/test_cuda_api_surface.py:60-105),
+which cross-checks api.hpp declarations against the .cu definitions and bindings.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from abstraction_regret_gb300 import build, native
+
+REPO = Path(__file__).resolve().parent.parent
+HEADER = REPO / "include" / "gbfsm.h"
+
+
+def declared() -> set[str]:
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    names = set(re.findall(r"\b(gbfsm_\w+)\s*\(", text))
+    return {n for n in names if not n.startswith("gbfsm_status")}
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.lib()
+
+
+def test_header_declares_the_reference_entry_points():
+    names = declared()
+    # one entry per _cuda.run_* of the reference (native/include/api.hpp:23-104)
+    for ref in ("dense", "bitpacked", "multistream", "multistream_shared", "multistream_async",
+                "worklist", "worklist_global", "worklist_warp", "worklist_compact",
+                "worklist_shared", "dfa"):
+        assert f"gbfsm_run_{ref}" in names
+    for dev in ("gbfsm_nfa_run", "gbfsm_dfa_run", "gbfsm_persistent_run",
+                "gbfsm_nfa_workspace_bytes", "gbfsm_last_error", "gbfsm_abi_version"):
+        assert dev in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(native.LIB_PATH)],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (gbfsm_\w+)", out))
+    missing = declared() - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    extra = {n for n in exported if n.startswith("gbfsm_")} - declared()
+    assert not extra, f"exported but not declared: {sorted(extra)}"
+
+
+def test_python_binding_covers_the_header(lib):
+    assert set(native.SIGNATURES) == declared()
+    assert lib.gbfsm_abi_version() == native.ABI_VERSION
+
+
+def test_struct_layouts_match_the_header():
+    assert ctypes.sizeof(native.Edge) == 16
+    assert ctypes.sizeof(native.Plan) == 32
+    assert ctypes.sizeof(native.Task) == 16
+    assert ctypes.sizeof(native.NfaDev) == 16 + 5 * 8 + 16
+    assert ctypes.sizeof(native.DfaDev) == 16 + 8 + 8 + 8
+
+
+def test_invalid_arguments_return_status_codes(lib):
+    plan = native.make_plan(native.TECH_COMPACT)
+    st = lib.gbfsm_nfa_run(None, None, None, 0, ctypes.byref(plan), None, None, None, None, 0,
+                           None)
+    assert st == native.INVALID_ARG
+    assert "NULL" in native.last_error()
+    d = native.NfaDev()
+    d.num_states, d.start_state, d.num_words = 10, 12, 1
+    st = lib.gbfsm_nfa_run(ctypes.byref(d), None, None, 0, ctypes.byref(plan), None, None, None,
+                           None, 0, None)
+    assert st == native.INVALID_ARG and "start_state" in native.last_error()
+    st = lib.gbfsm_dfa_layout(10, None, None, 3, None, None, None, None)
+    assert st == native.INVALID_ARG
+    dummy = ctypes.c_int32(0)
+    p = ctypes.addressof(dummy)
+    st = lib.gbfsm_dfa_layout(40000, p, p, 2, p, p, p, None)
+    assert st == native.UNSUPPORTED
+    assert lib.gbfsm_nfa_workspace_bytes(None, 10, None) == 0
+
+
+def test_status_mapping_raises_the_reference_exception_types():
+    with pytest.raises(ValueError):
+        native.check(native.INVALID_ARG, "x")
+    with pytest.raises(RuntimeError):
+        native.check(native.CUDA_ERROR, "x")
+    with pytest.raises(MemoryError):
+        native.check(native.OOM, "x")
+    with pytest.raises(TimeoutError):
+        native.check(native.TIMEOUT, "x")
+    native.check(native.OK, "x")
+
+
+def test_workload_walk_is_deterministic_and_thread_independent(lib):
+    from abstraction_regret_gb300 import workloads as W
+
+    nfa = W.random_nfa(300, seed=5, poisson=3.0, accept_prob=0.01)
+    off = W.offsets_of(np.array([0, 17, 4096, 1, 999], dtype=np.int64))
+    a = W.walk_bytes(nfa, off, seed=3, threads=1)
+    b = W.walk_bytes(nfa, off, seed=3, threads=5)
+    assert a.tobytes() == b.tobytes()
+    assert W.walk_bytes(nfa, off, seed=4).tobytes() != a.tobytes()

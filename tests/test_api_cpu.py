@@ -1,0 +1,173 @@
+"""Host-side mirror of the reference interface, without a GPU.
+
+Follows the reference's own CPU tests for the same surface: data model and builders
+(tests/test_nfa.py, test_validation.py), packing (test_packing.py:37-96), registry and
+dispatch (test_registry.py:47-172), result/benchmark conventions (test_api.py).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import abstraction_regret_gb300 as G
+from abstraction_regret_gb300 import registry as R
+from abstraction_regret_gb300.packing import (
+    WORD_BITS,
+    accept_bitmask,
+    pack_accept,
+    pack_bytes,
+    pack_inputs,
+    symbols,
+    words_for,
+)
+from abstraction_regret_gb300.result import BenchmarkStats, Result, batch_results
+
+
+def _nfa(accepting=(), n=8):
+    b = G.NFABuilder()
+    for i in range(n):
+        b.add_state(accept=i in accepting)
+    b.set_start(0)
+    return b.build()
+
+
+@pytest.mark.parametrize(("n", "w"), [(1, 1), (63, 1), (64, 1), (65, 2), (128, 2), (129, 3),
+                                      (500, 8)])
+def test_words_for_rounds_up(n, w):
+    assert words_for(n) == w
+
+
+def test_symbols_and_pack_inputs_match_the_reference_layout():
+    assert symbols(b"\x00A\xff").tolist() == [0, 65, 255]
+    assert symbols(b"\x00A\xff").dtype == np.int32
+    data, off = pack_inputs([b"ab", b"", b"xyz"])
+    assert off.tolist() == [0, 2, 2, 5] and off.dtype == np.int32 and data.dtype == np.int32
+    data, off = pack_inputs([b"", b""])
+    assert data.size == 0 and off.tolist() == [0, 0, 0]
+    data, off = pack_inputs([])
+    assert data.size == 0 and off.tolist() == [0]
+
+
+def test_pack_bytes_is_uint8_int64_and_padded():
+    data, off = pack_bytes([b"ab", b"", b"xyz"])
+    assert data.dtype == np.uint8 and off.dtype == np.int64
+    assert off.tolist() == [0, 2, 2, 5]
+    assert data.size % 16 == 0 and bytes(data[:5]) == b"abxyz"
+    data, off = pack_bytes([])
+    assert off.tolist() == [0] and data.size == 16
+
+
+def test_pack_accept_spans_word_boundaries():
+    acc = {0, 31, 32, 63, 64, 127, 128, 199}
+    nfa = _nfa(acc, n=200)
+    w = pack_accept(nfa)
+    assert w.dtype == np.uint64 and w.size == words_for(200)
+    got = {s for s in range(200) if int(w[s // WORD_BITS]) >> (s % WORD_BITS) & 1}
+    assert got == acc
+    assert int(pack_accept(_nfa({1, 5, 6}))[0]) == accept_bitmask(_nfa({1, 5, 6})) == 0b1100010
+    assert pack_accept(_nfa({0}), nwords=8).size == 8
+    assert pack_accept(_nfa({3}), dtype=np.int64).dtype == np.int64
+
+
+def test_builder_validation_matches_the_reference():
+    b = G.NFABuilder()
+    with pytest.raises(ValueError):
+        b.build()
+    s = b.add_state()
+    with pytest.raises(IndexError):
+        b.add_transition(s, "a", 7)
+    with pytest.raises(ValueError):
+        b.add_transition(s, chr(256), s)
+    with pytest.raises(ValueError):
+        b.add_transition(s, "ab", s)
+    with pytest.raises(ValueError):
+        b.add_transition(s, 300, s)
+    b.add_transition(s, G.ANY_SYMBOL, s)
+    nfa = b.build()
+    assert nfa.uses_any_symbol and nfa.num_sym_transitions == 1
+    d = G.DFABuilder()
+    with pytest.raises(ValueError):
+        d.build()
+    d.add_state()
+    with pytest.raises(IndexError):
+        d.add_transition(-1, 1, 0)
+    with pytest.raises(ValueError):
+        d.add_transition(0, 256, 0)
+    dfa = d.build()
+    assert dfa.num_states == 2 and dfa.trans.tolist() == [1] * 512  # the dead state
+
+
+def test_random_dfa_matches_the_reference_draws():
+    a = G.random_dfa(64, accept_prob=0.2, seed=3)
+    rng = np.random.default_rng(3)
+    assert np.array_equal(a.trans, rng.integers(0, 64, size=64 * 256, dtype=np.int32))
+    acc = rng.random(64) < 0.2
+    acc[0] = False
+    assert np.array_equal(a.accept, acc)
+
+
+def test_nfa_from_edges_equals_the_builder():
+    b = G.NFABuilder()
+    for i in range(4):
+        b.add_state(accept=i == 3)
+    for s, c, t in [(0, 1, 1), (2, 5, 3), (0, 9, 2), (1, 256, 0)]:
+        b.add_transition(s, c, t)
+    b.add_epsilon(1, 2)
+    ref = b.build()
+    got = G.nfa_from_edges(4, 0, ref.accept, [0, 2, 0, 1], [1, 5, 9, 256], [1, 3, 2, 0], [1], [2])
+    for f in ("sym_row_ptr", "sym_targets", "sym_symbols", "eps_row_ptr", "eps_targets"):
+        assert np.array_equal(getattr(got, f), getattr(ref, f)), f
+
+
+def test_kind_dispatch_and_identity_hashing():
+    nfa, dfa = _nfa(), G.random_dfa(4)
+    assert G.Kind.of(nfa) is G.Kind.NFA and G.Kind.of(dfa) is G.Kind.DFA
+    with pytest.raises(TypeError, match="expected an NFA or a DFA"):
+        G.Kind.of("nope")
+    assert {nfa: 1}[nfa] == 1 and {dfa: 2}[dfa] == 2
+    assert nfa != _nfa()
+
+
+def test_cuda_registers_both_kinds_with_declared_defaults():
+    assert R.list_kinds(G.Backend.CUDA) == [G.Kind.NFA, G.Kind.DFA]
+    assert "worklist_warp" in R.list_techniques(G.Backend.CUDA, G.Kind.NFA)
+    assert R.get_factory(G.Kind.NFA, G.Backend.CUDA, None)[0] == "auto"
+    assert R.get_factory(G.Kind.DFA, G.Backend.CUDA, None)[0] == "gather"
+    pairs = {(k, b) for k, b, _ in R._REGISTRY}
+    assert all(p in R._DEFAULTS for p in pairs)
+    for (k, b), t in R._DEFAULTS.items():
+        assert (k, b, t) in R._REGISTRY
+
+
+def test_registry_errors_name_the_alternatives():
+    with pytest.raises(KeyError, match="available: "):
+        R.get_factory(G.Kind.DFA, G.Backend.CUDA, "bitmap")
+    with pytest.raises(KeyError, match="has no nfa technique"):
+        G.run(_nfa(), b"a", backend="cpu")
+    with pytest.raises(RuntimeError, match="two defaults"):
+        R.register(G.Kind.NFA, G.Backend.CUDA, "something_else", default=True)(lambda a, t: None)
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """Without a device the CUDA path fails loudly instead of computing on the host."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert not G.is_available(G.Backend.CUDA)
+    assert "CUDA device" in (R.unavailable_reason(G.Backend.CUDA) or "")
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        G.run(_nfa({1}), b"a")
+
+
+def test_batch_results_and_benchmark_stats_conventions():
+    res = batch_results([1, 0, 1], [3, 0, 0], kernel_ms=2.0, transfer_ms=0.5)
+    assert [r.kernel_ms for r in res] == [2.0, 0.0, 0.0]
+    assert res[0].total_ms == 2.5 and res[1].total_ms == 0.0
+    assert res[0].matches(Result(True, 3)) and not res[0].matches(Result(True, 4))
+    st = BenchmarkStats("cuda", "auto", True, 3, 3, [1.0, 2.0, 3.0])
+    assert st.mean_ms == 2.0 and st.std_ms == pytest.approx(1.0)
+    assert st.as_row()["backend"] == "cuda"
+    with pytest.raises(ValueError):
+        G.benchmark(_nfa(), b"a", repeats=0)

@@ -1,0 +1,241 @@
+"""Bit-exact parity of every CUDA technique with the reference's oracle (GPU).
+
+Verdicts are integers, so the tolerance is zero: every ``(accepted, match_len)`` must
+equal the golden verdict (produced by the reference's ``simulate`` / ``simulate_dfa``)
+or the CPU oracle's on the same seeded inputs. All calls go through the C ABI of
+libgbfsm (the executors call ``gbfsm_nfa_run`` / ``gbfsm_dfa_run`` /
+``gbfsm_persistent_run``; the host-array entry points are called directly).
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import abstraction_regret_gb300 as G
+from abstraction_regret_gb300 import native
+from abstraction_regret_gb300 import workloads as W
+from abstraction_regret_gb300.engine import NfaChoice, PersistentEngine
+from abstraction_regret_gb300.executors import CudaDFAExecutor, CudaNFAExecutor
+from abstraction_regret_gb300.packing import pack_accept, pack_inputs
+from oracle import oracle as O
+
+from .golden_data import grouped
+
+pytestmark = pytest.mark.gpu
+
+NFA_TECHS = G.list_techniques(G.Backend.CUDA, G.Kind.NFA)
+DFA_TECHS = G.list_techniques(G.Backend.CUDA, G.Kind.DFA)
+
+
+def verdicts(results):
+    return [(r.accepted, r.match_len) for r in results]
+
+
+@pytest.mark.parametrize("technique", NFA_TECHS)
+def test_nfa_golden_corpus_every_technique(technique):
+    for a, cases in grouped("nfa"):
+        got = verdicts(G.run_batch(a, [d for _, d, _ in cases], technique=technique))
+        want = [tuple(v) for _, _, v in cases]
+        bad = [(cid, g, w) for (cid, _, _), g, w in zip(cases, got, want) if g != w]
+        assert not bad, f"{technique}: {bad[:3]}"
+
+
+@pytest.mark.parametrize("technique", DFA_TECHS)
+def test_dfa_golden_corpus_every_technique(technique):
+    for a, cases in grouped("dfa"):
+        got = verdicts(G.run_batch(a, [d for _, d, _ in cases], technique=technique))
+        want = [tuple(v) for _, _, v in cases]
+        assert got == want, technique
+
+
+def test_single_run_matches_batch_and_timing_convention():
+    a, cases = grouped("nfa")[0]
+    res = G.run_batch(a, [d for _, d, _ in cases])
+    assert res[0].kernel_ms > 0 and all(r.kernel_ms == 0 for r in res[1:])
+    for (_, d, v) in cases:
+        r = G.run(a, d)
+        assert (r.accepted, r.match_len) == tuple(v)
+
+
+def test_every_golden_automaton_in_one_persistent_launch():
+    """NFAs and DFAs of different sizes mixed in a single launch (the c4/c5 shape)."""
+    groups = grouped("nfa") + grouped("dfa")
+    automata = [a for a, _ in groups]
+    aut_ids, inputs, want = [], [], []
+    for k, (_, cases) in enumerate(groups):
+        for _, d, v in cases:
+            aut_ids.append(k)
+            inputs.append(d)
+            want.append(tuple(v))
+    for tech, cap in ((native.TECH_COMPACT, 8), (native.TECH_COMPACT, 128), (native.TECH_WARP, 0)):
+        choices = [NfaChoice(tech, max(cap, 1)) for _ in automata]
+        eng = PersistentEngine(automata, choices=choices, list_capacity=max(cap, 1))
+        flags, lens, ex, _, _ = eng.run_requests(aut_ids, inputs, with_examined=True)
+        got = list(zip(flags.astype(bool).tolist(), lens.tolist()))
+        assert got == want, (tech, cap)
+        assert all(0 <= e <= len(d) for e, d in zip(ex.tolist(), inputs))
+
+
+def test_empty_and_unaligned_batches():
+    a, cases = grouped("nfa")[5]
+    for tech in ("bitmap", "warp", "compact", "persistent"):
+        assert G.run_batch(a, [], technique=tech) == []
+        res = G.run_batch(a, [b"", b"", b""], technique=tech)
+        want = O.simulate(a, b"")
+        assert verdicts(res) == [want] * 3
+    dfa = G.random_dfa(300, accept_prob=0.01, seed=4)
+    rng = np.random.default_rng(1)
+    inputs = [rng.integers(0, 256, k, dtype=np.uint8).tobytes() for k in
+              (0, 1, 15, 16, 17, 31, 33, 255, 1000, 4099)]
+    for tech in DFA_TECHS:
+        assert verdicts(G.run_batch(dfa, inputs, technique=tech)) == [O.simulate_dfa(dfa, x) for x in inputs]
+
+
+def test_sparse_list_overflow_and_staging_paths():
+    """Small list capacities force sparse->dense->sparse switches mid-input."""
+    for a, cases in grouped("nfa")[-60:]:
+        inputs = [d for _, d, _ in cases]
+        want = [tuple(v) for _, _, v in cases]
+        for cap in (1, 2, 5):
+            for stage in (0, 1):
+                for threads in (32, 96):
+                    plan = native.make_plan(native.TECH_COMPACT, threads, cap, stage)
+                    ex = CudaNFAExecutor(a, plan=plan)
+                    assert verdicts(ex.run_batch(inputs)) == want, (cap, stage, threads)
+
+
+def _host_nfa_args(nfa):
+    arrs = [np.ascontiguousarray(getattr(nfa, f), dtype=np.int32) for f in
+            ("sym_row_ptr", "sym_targets", "sym_symbols", "eps_row_ptr", "eps_targets")]
+    return arrs, np.ascontiguousarray(pack_accept(nfa), dtype=np.uint64)
+
+
+def _ptr(a):
+    return a.ctypes.data if a.size else None
+
+
+@pytest.mark.parametrize("entry", ["gbfsm_run_multistream", "gbfsm_run_multistream_shared",
+                                   "gbfsm_run_multistream_async", "gbfsm_run_worklist",
+                                   "gbfsm_run_worklist_global", "gbfsm_run_worklist_warp",
+                                   "gbfsm_run_worklist_compact", "gbfsm_run_worklist_shared"])
+def test_reference_shaped_host_entry_points(entry):
+    """The C-ABI functions that stand in for _cuda.run_* (host arrays in and out)."""
+    lib = native.lib()
+    fn = getattr(lib, entry)
+    for a, cases in grouped("nfa")[::7]:
+        arrs, acc = _host_nfa_args(a)
+        data, off = pack_inputs([d for _, d, _ in cases])
+        n = len(cases)
+        flags = np.zeros(n, np.int32)
+        lens = np.zeros(n, np.int32)
+        ms = ctypes.c_float(0)
+        st = fn(*[_ptr(x) for x in arrs], _ptr(acc), _ptr(data), _ptr(off), n, a.num_states,
+                a.start_state, int(a.uses_any_symbol), _ptr(flags), _ptr(lens), ctypes.byref(ms))
+        native.check(st, entry)
+        assert list(zip(flags.astype(bool).tolist(), lens.tolist())) == [tuple(v) for *_, v in cases]
+        assert ms.value > 0
+
+
+def test_reference_shaped_single_and_dfa_entry_points():
+    lib = native.lib()
+    for a, cases in grouped("nfa")[::11]:
+        arrs, acc = _host_nfa_args(a)
+        acc8 = np.ascontiguousarray(a.accept, dtype=np.int8)
+        for _, d, v in cases:
+            syms = np.frombuffer(d, np.uint8).astype(np.int32)
+            for fn, accept in ((lib.gbfsm_run_dense, acc8), (lib.gbfsm_run_bitpacked, acc)):
+                f, l, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float()
+                st = fn(*[_ptr(x) for x in arrs], _ptr(accept), _ptr(syms), syms.size,
+                        a.num_states, a.start_state, 0, ctypes.byref(f), ctypes.byref(l),
+                        ctypes.byref(ms))
+                native.check(st, "single-input entry")
+                assert (bool(f.value), l.value) == tuple(v)
+    for a, cases in grouped("dfa"):
+        data, off = pack_inputs([d for _, d, _ in cases])
+        n = len(cases)
+        flags, lens, ms = np.zeros(n, np.int32), np.zeros(n, np.int32), ctypes.c_float()
+        trans = np.ascontiguousarray(a.trans, np.int32)
+        acc = np.ascontiguousarray(a.accept, np.int8)
+        st = lib.gbfsm_run_dfa(_ptr(trans), _ptr(acc), _ptr(data), _ptr(off), n, a.num_states,
+                               a.start_state, _ptr(flags), _ptr(lens), ctypes.byref(ms))
+        native.check(st, "gbfsm_run_dfa")
+        assert list(zip(flags.astype(bool).tolist(), lens.tolist())) == [tuple(v) for *_, v in cases]
+
+
+def test_invalid_automata_are_rejected_before_any_launch():
+    b = G.NFABuilder()
+    b.add_state()
+    good = b.build()
+    bad = G.NFA(num_states=1, start_state=0, accept=good.accept,
+                sym_row_ptr=np.array([0, 1], np.int32), sym_targets=np.array([3], np.int32),
+                sym_symbols=np.array([7], np.int32), eps_row_ptr=good.eps_row_ptr,
+                eps_targets=good.eps_targets)
+    with pytest.raises(ValueError, match="invalid NFA"):
+        CudaNFAExecutor(bad, "compact")
+    d = G.random_dfa(8)
+    bad_dfa = G.DFA(num_states=8, start_state=0, accept=d.accept, trans=d.trans.copy() + 8)
+    with pytest.raises(ValueError, match="invalid DFA"):
+        CudaDFAExecutor(bad_dfa)
+
+
+# ---- benchmark configurations at full size, against the C oracle ------------------------
+
+def _check_batch(b, runner, check_examined=True):
+    flags, lens, ex = runner(b)
+    for k, a in enumerate(b.automata):
+        sel = np.flatnonzero(b.aut_ids == k)
+        sb = b.subset(sel)
+        if hasattr(a, "trans"):
+            f, l, e = O.dfa_batch(a, sb.data, sb.offsets)
+        else:
+            f, l, e, _ = O.nfa_batch(a, sb.data, sb.offsets)
+        assert np.array_equal(flags[sel], f), b.name
+        assert np.array_equal(lens[sel], l), b.name
+        if check_examined:
+            assert np.array_equal(ex[sel], e), b.name
+
+
+def _persistent(b):
+    eng = PersistentEngine(b.automata)
+    f, l, e, _, _ = eng.run_requests(b.aut_ids, b.inputs(), with_examined=True)
+    return f, l, e
+
+
+def _plain(tech):
+    def run(b):
+        ex = G.executors.make_nfa_executor(b.automata[0], tech) if not hasattr(
+            b.automata[0], "trans") else G.executors.make_dfa_executor(b.automata[0], tech)
+        f, l, e, _, _ = ex.run_arrays(b.inputs(), with_examined=True)
+        return f, l, e
+    return run
+
+
+@pytest.mark.parametrize("variant", ["literal", "live", "sustained"])
+def test_c1_full(variant):
+    b = W.c1(variant)
+    for tech in ("bitmap", "warp", "compact", "persistent", "auto"):
+        _check_batch(b, _plain(tech))
+
+
+@pytest.mark.parametrize("variant", ["literal", "sustained"])
+def test_c2_full_or_bounded(variant):
+    b = W.c2(variant, n_inputs=4096 if variant == "literal" else 512)
+    for tech in DFA_TECHS:
+        _check_batch(b, _plain(tech))
+
+
+@pytest.mark.parametrize("variant", ["literal", "live", "sustained"])
+def test_c3_full(variant):
+    b = W.c3(variant)
+    _check_batch(b, _persistent)
+    _check_batch(b, _plain("compact"))
+
+
+@pytest.mark.parametrize("variant", ["literal", "live"])
+def test_c4_all_pairs_one_launch(variant):
+    b = W.c4(variant)
+    assert b.n_inputs == 1024
+    _check_batch(b, _persistent)
