@@ -50,8 +50,8 @@ PersistLayout persist_layout(int32_t max_words, const gbfsm_plan &p) {
 __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
     const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
     int32_t n_tasks, const int32_t *__restrict__ input_ids, const uint8_t *__restrict__ data,
-    const int64_t *__restrict__ offsets, int32_t *flags, int32_t *lens, int32_t *examined,
-    PersistLayout L, uint32_t *ticket, uint8_t *gws) {
+    const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends, int32_t *flags,
+    int32_t *lens, int32_t *examined, PersistLayout L, uint32_t *ticket, uint8_t *gws) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int warp = (int)(threadIdx.x >> 5);
     const uint32_t lane = lane_id();
@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
             const int32_t id = input_ids[task.first];
             const int64_t b = offsets[id];
-            const Verdict v = simulate_warp<false>(nfa, R, data + b, offsets[id + 1] - b, S);
+            const int64_t e = ends ? ends[id] : offsets[id + 1];
+            const Verdict v = simulate_warp<false>(nfa, R, data + b, e - b, S);
             if (lane == 0) {
                 flags[id] = v.flag;
                 lens[id] = v.len;
@@ -99,16 +100,17 @@ __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
             if ((int)lane < task.count) {
                 const int32_t id = input_ids[task.first + (int)lane];
                 const int64_t b = offsets[id];
+                const int64_t e = ends ? ends[id] : offsets[id + 1];
                 int32_t f, l;
                 int64_t ex;
                 if (d.entry_bytes == 2)
                     dfa_walk<uint16_t, false>(static_cast<const uint16_t *>(d.table), d.accept_bits,
-                                              (uint32_t)d.start_state, data + b,
-                                              offsets[id + 1] - b, f, l, ex);
+                                              (uint32_t)d.start_state, data + b, e - b, f,
+                                              l, ex);
                 else
                     dfa_walk<uint32_t, false>(static_cast<const uint32_t *>(d.table), d.accept_bits,
-                                              (uint32_t)d.start_state, data + b,
-                                              offsets[id + 1] - b, f, l, ex);
+                                              (uint32_t)d.start_state, data + b, e - b, f,
+                                              l, ex);
                 flags[id] = f;
                 lens[id] = l;
                 if (examined) examined[id] = (int32_t)ex;
@@ -174,8 +176,8 @@ int32_t persistent_ctas_query(const PersistLayout &L, const gbfsm_plan &p) {
 
 gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
-                               const uint8_t *data, const int64_t *offsets, int32_t *flags,
-                               int32_t *lens, int32_t *examined, void *workspace,
+                               const uint8_t *data, const int64_t *offsets, const int64_t *ends,
+                               int32_t *flags, int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream) {
     const PersistLayout L = persist_layout(max_words, p);
     if (L.wpc < 1 || L.wpc * 32 > kMaxBlockThreads || (p.block_threads % 32) != 0)
@@ -198,8 +200,8 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
     const int needed = (n_tasks + L.wpc - 1) / L.wpc;
     if (grid > needed) grid = needed;
     persistent_kernel<<<grid, L.wpc * 32, smem, stream>>>(table, tasks, n_tasks, input_ids, data,
-                                                          offsets, flags, lens, examined, L, ticket,
-                                                          gws);
+                                                          offsets, ends, flags, lens, examined, L,
+                                                          ticket, gws);
     GBFSM_LAUNCH_CHECK("persistent_kernel launch");
     return GBFSM_OK;
 }

@@ -131,16 +131,27 @@ class PersistentEngine:
 
     # ---- launches -------------------------------------------------------------------------
 
+    def new_workspace(self) -> torch.Tensor:
+        """A separate workspace (queue ticket + dense scratch) for a concurrent launch."""
+        return torch.zeros(self.ws_bytes, dtype=torch.uint8, device=self.device)
+
     def launch(self, d_data, d_off, d_tasks, n_tasks, d_ids, d_flags, d_lens, d_examined=None,
-               stream=None) -> None:
-        """Enqueue the persistent launch (device pointers only; no synchronisation)."""
+               stream=None, d_ends=None, workspace=None) -> None:
+        """Enqueue the persistent launch (no synchronisation).
+
+        ``d_data`` is a device tensor or a raw address (e.g. of pinned host memory the
+        device reads directly); with ``d_ends`` input i spans ``[d_off[i], d_ends[i])``.
+        """
         stream = stream or torch.cuda.current_stream(self.device)
+        ws = self.workspace if workspace is None else workspace
+        data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
         st = native.lib().gbfsm_persistent_run(
             self.table.data_ptr(), len(self.automata), self.max_words, d_tasks.data_ptr(),
-            int(n_tasks), d_ids.data_ptr(), d_data.data_ptr(), d_off.data_ptr(),
+            int(n_tasks), d_ids.data_ptr(), data_ptr, d_off.data_ptr(),
+            d_ends.data_ptr() if d_ends is not None else None,
             d_flags.data_ptr(), d_lens.data_ptr(),
             d_examined.data_ptr() if d_examined is not None else None,
-            self.workspace.data_ptr(), self.ws_bytes, ctypes.byref(self.plan), stream.cuda_stream)
+            ws.data_ptr(), self.ws_bytes, ctypes.byref(self.plan), stream.cuda_stream)
         native.check(st, "gbfsm_persistent_run")
 
     def _upload_tasks(self, tasks: np.ndarray, ids: np.ndarray, stream):

@@ -113,7 +113,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_persistent_workspace_bytes": (_sz, [_i32, _P(Plan)]),
     "gbfsm_persistent_ctas_per_sm": (_i32, [_i32, _P(Plan)]),
     "gbfsm_persistent_run": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
-                                            _vp, _vp, _sz, _P(Plan), _vp]),
+                                            _vp, _vp, _vp, _sz, _P(Plan), _vp]),
     "gbfsm_run_multistream": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_shared": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_async": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
@@ -129,6 +129,7 @@ SIGNATURES: dict[str, tuple] = {
                             [_P(Plan)] + [_vp] * 3),
     "gbfsm_run_dfa_bytes": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                            _vp]),
+    "gbfsm_host_device_pointer": (ctypes.c_int, [_vp, _P(_vp)]),
     "gbfsm_workload_walk": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _u64, _vp, _i32]),
 }
 
@@ -174,6 +175,13 @@ def check(status: int, what: str) -> None:
     if status == TIMEOUT:
         raise TimeoutError(msg)
     raise RuntimeError(msg)
+
+
+def device_pointer(host_ptr: int) -> int:
+    """Device address of page-locked host memory at ``host_ptr`` (raises if not mapped)."""
+    out = ctypes.c_void_p()
+    check(lib().gbfsm_host_device_pointer(host_ptr, ctypes.byref(out)), "gbfsm_host_device_pointer")
+    return int(out.value or 0)
 
 
 def make_plan(technique: int, block_threads: int = 0, list_capacity: int = 0, stage: int = 0,

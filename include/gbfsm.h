@@ -208,15 +208,24 @@ typedef struct gbfsm_task {
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan);
 
-/* Run `n_tasks` tasks. table/tasks/input_ids are device arrays. Results are written by
- * input index. workspace (device, >= gbfsm_persistent_workspace_bytes) holds the queue
- * ticket, which this call resets in-stream, so the launch can be replayed from a graph. */
+/* Run `n_tasks` tasks. table/tasks/input_ids are device arrays. Input i is
+ * data[offsets[i] .. ends[i]) when `ends` is non-NULL (spans anywhere in `data`, e.g.
+ * requests left in place in a pinned host pool that the device reads directly), else
+ * data[offsets[i] .. offsets[i+1]). Results are written by input index. workspace
+ * (device, >= gbfsm_persistent_workspace_bytes) holds the queue ticket, which this call
+ * resets in-stream, so the launch can be replayed from a graph; concurrent launches need
+ * separate workspaces. */
 gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automata,
                                   int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
                                   const int32_t *input_ids, const uint8_t *data,
-                                  const int64_t *offsets, int32_t *flags, int32_t *lens,
-                                  int32_t *examined, void *workspace, size_t workspace_bytes,
-                                  const gbfsm_plan *plan, void *stream);
+                                  const int64_t *offsets, const int64_t *ends, int32_t *flags,
+                                  int32_t *lens, int32_t *examined, void *workspace,
+                                  size_t workspace_bytes, const gbfsm_plan *plan, void *stream);
+
+/* Device address of page-locked host memory (cudaHostGetDevicePointer), for kernels that
+ * read request bytes in place over the host link instead of copying them first. No
+ * counterpart in the reference (which copies every input, common.cuh:150-159). */
+gbfsm_status gbfsm_host_device_pointer(void *host, void **device);
 
 /* Occupancy query for persistent launches: CTAs of `plan` resident per SM. */
 int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan);
