@@ -84,7 +84,7 @@ gbfsm_status launch_dfa_walk(const gbfsm_dfa_dev &d, const gbfsm_plan &p, const 
         if (threads > 256) threads = 256;
     }
     if (threads % 32 != 0 || threads > kMaxBlockThreads)
-        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 512 (got %d)",
+        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 256 (got %d)",
                     threads);
     const size_t budget = (size_t)smem_optin() - kSmemReserve;
     const bool staged = p.stage && (16u + (size_t)pad16(d.table_bytes) <= budget);

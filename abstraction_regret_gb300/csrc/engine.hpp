@@ -11,7 +11,7 @@
 namespace gbfsm {
 
 constexpr int kDefaultListCapacity = 128;
-constexpr int kMaxBlockThreads = 512;  // __launch_bounds__ of every simulation kernel
+constexpr int kMaxBlockThreads = 256;  // __launch_bounds__ of every simulation kernel
 constexpr size_t kSmemReserve = 1024;  // static/driver-reserved shared memory headroom
 
 // Where the per-warp scratch of the warp simulator lives, and how shared memory is laid

@@ -242,46 +242,268 @@ __device__ __forceinline__ int bitmap_to_list(const gbfsm_nfa_dev &A, const Rows
     return n;
 }
 
+// Position of the k-th (0-based) set bit of `mask` (k < popc(mask)): binary search on
+// popcounts, no shuffles.
+__device__ __forceinline__ uint32_t select_bit(uint32_t mask, uint32_t k) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w; w >>= 1) {
+        const uint32_t c = __popc((mask >> pos) & ((1u << w) - 1u));
+        if (k >= c) {
+            k -= c;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+__device__ __forceinline__ uint4 shfl_rec(const uint4 &r, uint32_t src) {
+    return make_uint4(__shfl_sync(GBFSM_FULL_MASK, r.x, src), __shfl_sync(GBFSM_FULL_MASK, r.y, src),
+                      __shfl_sync(GBFSM_FULL_MASK, r.z, src), __shfl_sync(GBFSM_FULL_MASK, r.w, src));
+}
+
+enum StepEvent { kAlive = 0, kDead = 1, kAccept = 2 };
+
+// One warp's NFA run, advanced one byte at a time. Three representations of the
+// current set, chosen per step:
+//   REG   up to 32 members, member i's record held by lane i in registers; a step whose
+//         members have at most 32 edges in total is one edge load per lane, deduplicated
+//         with __match_any_sync and compacted with ballot/popc/select + shuffles;
+//   LIST  up to C members in the shared list LA (steps through walk_batch and V);
+//   DENSE the packed bitmap D (all W words scanned per step).
+// V, FA, FB are all-zero between steps; D is all-zero unless the mode is DENSE.
+template <bool kStaged>
+struct WarpNfa {
+    const gbfsm_nfa_dev &A;
+    const Rows &R;
+    WarpScratch S;
+    int W;
+    bool has_eps;
+    int mode;  // 0 REG, 1 LIST, 2 DENSE
+    int m;
+    uint4 mine;
+
+    static constexpr int kReg = 0, kList = 1, kDense = 2;
+
+    __device__ __forceinline__ WarpNfa(const gbfsm_nfa_dev &a, const Rows &r, WarpScratch s)
+        : A(a), R(r), S(s), W(a.num_words), has_eps((a.flags & GBFSM_NFA_HAS_EPS) != 0),
+          mode(kReg), m(0), mine(make_uint4(0, 0, 0, 0)) {}
+
+    __device__ __forceinline__ uint4 state_record(uint32_t s) const {
+        uint32_t info = 0;
+        if ((A.accept_words[s >> 6] >> (s & 63u)) & 1ull) info |= GBFSM_EDGE_ACCEPT;
+        if (has_eps && load_row<kStaged>(R.eps_row + s + 1) > load_row<kStaged>(R.eps_row + s))
+            info |= GBFSM_EDGE_HAS_EPS;
+        return make_uint4(s, info, load_row<kStaged>(R.sym_row + s),
+                          load_row<kStaged>(R.sym_row + s + 1));
+    }
+
+    // The set just built in V (n members; LB holds them when !dense_now) becomes current.
+    __device__ int finish_general(int n, bool dense_now, uint32_t info_or) {
+        const uint32_t lane = lane_id();
+        __syncwarp();
+        const uint32_t flags = __reduce_or_sync(GBFSM_FULL_MASK, info_or);
+        if (!dense_now) {
+            for (int j = (int)lane; j < n; j += 32) S.V[S.LB[j].x >> 6] = 0ull;
+            __syncwarp();
+            if (n <= 32) {
+                mine = ((int)lane < n) ? S.LB[lane] : make_uint4(0, 0, 0, 0);
+                mode = kReg;
+            } else {
+                uint4 *t = S.LA;
+                S.LA = S.LB;
+                S.LB = t;
+                mode = kList;
+            }
+        } else {
+            uint64_t *t = S.D;  // the new set becomes D; the old D (stale or zero) is cleared
+            S.D = S.V;
+            S.V = t;
+            __syncwarp();
+            zero_words(S.V, W);
+            mode = kDense;
+            if (S.C > 0 && 2 * n <= S.C) {
+                __syncwarp();
+                n = bitmap_to_list<kStaged>(A, R, S.D, W, S.LA);
+                __syncwarp();
+                if (n <= 32) {
+                    mine = ((int)lane < n) ? S.LA[lane] : make_uint4(0, 0, 0, 0);
+                    mode = kReg;
+                } else {
+                    mode = kList;
+                }
+            }
+        }
+        m = n;
+        __syncwarp();
+        return (flags & GBFSM_EDGE_ACCEPT) ? kAccept : kAlive;
+    }
+
+    // Start configuration: closure({start}).
+    __device__ int init_start() {
+        const uint4 rec = state_record((uint32_t)A.start_state);
+        if (S.C > 0 && !(rec.y & GBFSM_EDGE_HAS_EPS)) {
+            mode = kReg;
+            m = 1;
+            mine = lane_id() == 0 ? rec : make_uint4(0, 0, 0, 0);
+            return (rec.y & GBFSM_EDGE_ACCEPT) ? kAccept : kAlive;
+        }
+        const uint32_t s = rec.x;
+        if (lane_id() == 0) {
+            S.V[s >> 6] |= 1ull << (s & 63u);
+            if (S.C > 0) S.LB[0] = rec;
+        }
+        __syncwarp();
+        uint32_t info_or = rec.y;
+        int n = 1;
+        bool dense_now = S.C == 0;
+        if (has_eps && !dense_now) n = sparse_closure<kStaged>(R, S.LB, n, S.C, S.V, info_or);
+        if (n > S.C) dense_now = true;
+        if (has_eps && dense_now) {
+            __syncwarp();
+            n += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
+        }
+        return finish_general(n, dense_now, info_or);
+    }
+
+    __device__ int step_general(uint32_t sym) {
+        const uint32_t lane = lane_id();
+        if (mode == kReg) {
+            if (m <= S.C) {
+                if ((int)lane < m) S.LA[lane] = mine;
+                mode = kList;
+            } else {  // more members than the list holds: spill to the bitmap
+                if ((int)lane < m)
+                    atomicOr(reinterpret_cast<unsigned long long *>(S.D + (mine.x >> 6)),
+                             1ull << (mine.x & 63u));
+                mode = kDense;
+            }
+            __syncwarp();
+        }
+        uint32_t info_or = 0;
+        bool dense_now = mode == kDense;
+        int n;
+        if (!dense_now)
+            n = sparse_expand<kStaged>(R, S.LA, m, sym, S.V, S.LB, S.C, info_or);
+        else
+            n = dense_expand<kStaged>(R, S.D, W, true, sym, R.sym_edges, R.sym_row, S.V, nullptr,
+                                      info_or);
+        if (n == 0) {  // reference.py:59-60: the set died
+            if (dense_now) {
+                __syncwarp();
+                zero_words(S.D, W);
+            }
+            mode = kReg;
+            m = 0;
+            __syncwarp();
+            return kDead;
+        }
+        __syncwarp();
+        if (has_eps && (__reduce_or_sync(GBFSM_FULL_MASK, info_or) & GBFSM_EDGE_HAS_EPS)) {
+            if (!dense_now && n <= S.C) n = sparse_closure<kStaged>(R, S.LB, n, S.C, S.V, info_or);
+            if (dense_now || n > S.C) {
+                __syncwarp();
+                n += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
+                dense_now = true;
+            }
+        }
+        if (n > S.C) dense_now = true;
+        return finish_general(n, dense_now, info_or);
+    }
+
+    // REG-mode step: at most 32 members with at most 32 edges in total.
+    __device__ int step_reg(uint32_t sym) {
+        const uint32_t lane = lane_id();
+        const uint32_t deg = ((int)lane < m) ? mine.w - mine.z : 0u;
+        const uint32_t incl = warp_inclusive_scan(deg);
+        const uint32_t total = __shfl_sync(GBFSM_FULL_MASK, incl, 31);
+        if (total > 32u) return step_general(sym);
+        const uint32_t excl = incl - deg;
+        uint32_t owner = 0;
+        if (m > 1) {
+#pragma unroll
+            for (uint32_t step = 16; step >= 1; step >>= 1) {
+                const uint32_t cand = owner + step;
+                const uint32_t e = __shfl_sync(GBFSM_FULL_MASK, excl, cand);
+                if (e <= lane) owner = cand;
+            }
+        }
+        const uint32_t orb = __shfl_sync(GBFSM_FULL_MASK, mine.z, owner);
+        const uint32_t oex = __shfl_sync(GBFSM_FULL_MASK, excl, owner);
+        bool match = false;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        if (lane < total) {
+            rec = load_edge<kStaged>(R.sym_edges + orb + (lane - oex));
+            const uint32_t es = rec.y & GBFSM_EDGE_SYMBOL_MASK;
+            match = (es == sym) || (es == GBFSM_ANY_SYMBOL);
+        }
+        const uint32_t key = match ? rec.x : 0xffffffffu;
+        const uint32_t grp = __match_any_sync(GBFSM_FULL_MASK, key);
+        const bool fresh = match && ((uint32_t)(__ffs(grp) - 1) == lane);
+        const uint32_t F = __ballot_sync(GBFSM_FULL_MASK, fresh);
+        const int n = __popc(F);
+        if (n == 0) {  // reference.py:59-60
+            m = 0;
+            return kDead;
+        }
+        const uint32_t acc = __ballot_sync(GBFSM_FULL_MASK, fresh && (rec.y & GBFSM_EDGE_ACCEPT));
+        if (has_eps && __ballot_sync(GBFSM_FULL_MASK, fresh && (rec.y & GBFSM_EDGE_HAS_EPS))) {
+            // epsilon closure needed: continue through the shared-memory path
+            if (fresh) {
+                const int pos = __popc(F & lanemask_lt());
+                if (pos < S.C) S.LB[pos] = rec;
+                atomicOr(reinterpret_cast<unsigned long long *>(S.V + (rec.x >> 6)),
+                         1ull << (rec.x & 63u));
+            }
+            __syncwarp();
+            uint32_t info_or = fresh ? rec.y : 0u;
+            int nn = n;
+            bool dense_now = false;
+            if (nn <= S.C) nn = sparse_closure<kStaged>(R, S.LB, nn, S.C, S.V, info_or);
+            if (nn > S.C) {
+                __syncwarp();
+                nn += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
+                dense_now = true;
+            }
+            return finish_general(nn, dense_now, info_or);
+        }
+        const uint32_t src = select_bit(F, min(lane, (uint32_t)(n - 1)));
+        mine = shfl_rec(rec, src);
+        if ((int)lane >= n) mine = make_uint4(0, 0, 0, 0);
+        m = n;
+        return acc ? kAccept : kAlive;
+    }
+
+    __device__ __forceinline__ int step(uint32_t sym) {
+        return mode == kReg ? step_reg(sym) : step_general(sym);
+    }
+
+    // Leave V, D, FA and FB all-zero for the next input.
+    __device__ void cleanup() {
+        __syncwarp();
+        if (mode == kDense) {
+            zero_words(S.D, W);
+            zero_words(S.V, W);
+        }
+        mode = kReg;
+        m = 0;
+        __syncwarp();
+    }
+};
+
 // Simulate one input with a whole warp. All lanes call it with identical arguments and
 // all receive the verdict. `R` may point at shared-memory copies of the edge rows.
 template <bool kStaged>
 __device__ Verdict simulate_warp(const gbfsm_nfa_dev &A, const Rows &R, const uint8_t *in,
                                  int64_t len, WarpScratch S) {
-    const int W = A.num_words;
-    const bool has_eps = (A.flags & GBFSM_NFA_HAS_EPS) != 0;
-    const int C = S.C;
+    WarpNfa<kStaged> w(A, R, S);
     Verdict v{0, 0, 0};
-
-    // ---- start configuration: closure({start}) --------------------------------------
-    uint32_t info_or = 0;
-    int m = 0;
-    bool dense = (C == 0);
-    {
-        const uint32_t s = (uint32_t)A.start_state;
-        uint32_t info = 0;
-        if ((A.accept_words[s >> 6] >> (s & 63u)) & 1ull) info |= GBFSM_EDGE_ACCEPT;
-        if (has_eps && load_row<kStaged>(R.eps_row + s + 1) > load_row<kStaged>(R.eps_row + s))
-            info |= GBFSM_EDGE_HAS_EPS;
-        const uint4 rec = make_uint4(s, info, load_row<kStaged>(R.sym_row + s),
-                                     load_row<kStaged>(R.sym_row + s + 1));
-        if (lane_id() == 0) {
-            S.V[s >> 6] |= 1ull << (s & 63u);
-            if (C > 0) S.LB[0] = rec;
-        }
-        info_or = info;
-        m = 1;
-        __syncwarp();
-        if (has_eps) {
-            if (!dense) m = sparse_closure<kStaged>(R, S.LB, m, C, S.V, info_or);
-            if (dense || m > C) {
-                __syncwarp();
-                m += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
-                dense = true;
-            }
-        }
+    int ev = w.init_start();
+    if (ev == kAccept) {
+        v.flag = 1;
+        w.cleanup();
+        return v;
     }
-
-    int64_t pos = 0;  // bytes consumed so far
     // input bytes: 16-byte blocks, the next block loaded one block ahead of use
     const uint8_t *end = in + len;
     const uint64_t addr = reinterpret_cast<uint64_t>(in);
@@ -290,44 +512,9 @@ __device__ Verdict simulate_warp(const gbfsm_nfa_dev &A, const Rows &R, const ui
     uint4 chunk = make_uint4(0, 0, 0, 0), ahead = make_uint4(0, 0, 0, 0);
     if (len > 0) chunk = ld_stream16(blk);
     if (blk + 16 < end) ahead = ld_stream16(blk + 16);
-
-    for (;;) {
-        // ---- finish the step that produced the set now in V (members m) --------------
-        __syncwarp();
-        const uint32_t flags = __reduce_or_sync(GBFSM_FULL_MASK, info_or);
-        if (flags & GBFSM_EDGE_ACCEPT) {
-            v.flag = 1;
-            v.len = (int32_t)pos;
-            v.examined = pos;
-            break;
-        }
-        if (!dense) {
-            // V holds exactly LB[0..m): clear it, LB becomes the current list
-            for (int j = (int)lane_id(); j < m; j += 32) S.V[S.LB[j].x >> 6] = 0ull;
-            uint4 *t = S.LA;
-            S.LA = S.LB;
-            S.LB = t;
-        } else {
-            // V becomes the current set; the old current set (all-zero while sparse,
-            // stale while dense) is cleared to serve as the next V
-            uint64_t *t = S.D;
-            S.D = S.V;
-            S.V = t;
-            __syncwarp();
-            zero_words(S.V, W);
-            if (C > 0 && 2 * m <= C) {
-                __syncwarp();
-                m = bitmap_to_list<kStaged>(A, R, S.D, W, S.LA);
-                dense = false;
-            }
-        }
-        __syncwarp();
-        if (pos >= len) {
-            v.examined = len;
-            break;
-        }
-
-        // ---- next byte ------------------------------------------------------------
+    int64_t pos = 0;
+    v.examined = len;
+    while (pos < len) {
         if (k == 16) {
             blk += 16;
             k = 0;
@@ -337,49 +524,19 @@ __device__ Verdict simulate_warp(const gbfsm_nfa_dev &A, const Rows &R, const ui
         const uint32_t sym = byte_of(chunk, k);
         ++k;
         ++pos;
-
-        info_or = 0;
-        int n;
-        if (!dense) {
-            n = sparse_expand<kStaged>(R, S.LA, m, sym, S.V, S.LB, C, info_or);
-        } else {
-            n = dense_expand<kStaged>(R, S.D, W, true, sym, R.sym_edges, R.sym_row, S.V, nullptr,
-                                      info_or);
-        }
-        if (n == 0) {  // reference.py:59-60: the set died
+        ev = w.step(sym);
+        if (ev == kDead) {
             v.examined = pos;
-            if (dense) {
-                __syncwarp();
-                zero_words(S.D, W);
-            }
             break;
         }
-        __syncwarp();
-        if (has_eps && (__reduce_or_sync(GBFSM_FULL_MASK, info_or) & GBFSM_EDGE_HAS_EPS)) {
-            if (!dense && n <= C) n = sparse_closure<kStaged>(R, S.LB, n, C, S.V, info_or);
-            if (dense || n > C) {
-                __syncwarp();
-                n += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
-            }
+        if (ev == kAccept) {
+            v.flag = 1;
+            v.len = (int32_t)pos;
+            v.examined = pos;
+            break;
         }
-        if (!dense && n > C) {
-            // the list overflowed: V holds the whole set; continue in dense form
-            dense = true;
-        }
-        m = n;
     }
-
-    // leave the scratch all-zero for the next input
-    __syncwarp();
-    if (!dense) {
-        if (v.flag) {
-            for (int j = (int)lane_id(); j < m; j += 32) S.V[S.LB[j].x >> 6] = 0ull;
-        }
-    } else {
-        zero_words(S.V, W);
-        zero_words(S.D, W);
-    }
-    __syncwarp();
+    w.cleanup();
     return v;
 }
 

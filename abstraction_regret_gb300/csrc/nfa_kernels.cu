@@ -77,13 +77,13 @@ __global__ void __launch_bounds__(kMaxBlockThreads) nfa_warp_kernel(gbfsm_nfa_de
     uint8_t *gp = gws + (size_t)input * wp.global_per_warp;
     WarpScratch S;
     S.C = wp.C;
-    uint8_t *&vp = wp.v_in_smem ? sp : gp;
+    // V and the lists first, then D/FA/FB, each in shared memory or the global slice
+    const size_t vpart = wbytes + (size_t)32u * (uint32_t)wp.C;
+    uint8_t *vp = wp.v_in_smem ? sp : gp;
+    uint8_t *dp = wp.dense_in_smem ? sp + vpart : (wp.v_in_smem ? gp : gp + vpart);
     S.V = reinterpret_cast<uint64_t *>(vp);
-    vp += wbytes;
-    S.LA = reinterpret_cast<uint4 *>(vp);
+    S.LA = reinterpret_cast<uint4 *>(vp + wbytes);
     S.LB = S.LA + wp.C;
-    vp += (size_t)32u * (uint32_t)wp.C;
-    uint8_t *&dp = wp.dense_in_smem ? sp : gp;
     S.D = reinterpret_cast<uint64_t *>(dp);
     S.FA = reinterpret_cast<uint64_t *>(dp + wbytes);
     S.FB = reinterpret_cast<uint64_t *>(dp + 2 * wbytes);
@@ -332,7 +332,7 @@ gbfsm_status make_warp_plan(const gbfsm_nfa_dev &a, int32_t n_inputs, const gbfs
                                             : kDefaultListCapacity;
     int threads = p.block_threads > 0 ? p.block_threads : 128;
     if (threads % 32 != 0 || threads > kMaxBlockThreads)
-        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 512 (got %d)",
+        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 256 (got %d)",
                     threads);
     wp.warps_per_cta = threads / 32;
     const size_t budget = (size_t)smem_optin() - kSmemReserve;
@@ -373,7 +373,7 @@ gbfsm_status make_bitmap_plan(const gbfsm_nfa_dev &a, int32_t n_inputs, const gb
     bp.W = a.num_words;
     int threads = p.block_threads > 0 ? p.block_threads : 128;
     if (threads % 32 != 0 || threads > kMaxBlockThreads)
-        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 512 (got %d)",
+        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 256 (got %d)",
                     threads);
     const size_t budget = (size_t)smem_optin() - kSmemReserve;
     const size_t per_thread = (size_t)bp.W * 32u;

@@ -181,7 +181,7 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream) {
     const PersistLayout L = persist_layout(max_words, p);
     if (L.wpc < 1 || L.wpc * 32 > kMaxBlockThreads || (p.block_threads % 32) != 0)
-        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 512");
+        return fail(GBFSM_INVALID_ARG, "block_threads must be a multiple of 32 up to 256");
     const int ctas = persistent_ctas_per_sm(max_words, p);
     if (ctas <= 0)
         return fail(GBFSM_UNSUPPORTED,
