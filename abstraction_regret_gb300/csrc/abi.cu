@@ -236,7 +236,8 @@ int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan) 
 gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automata,
                                   int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
                                   const int32_t *input_ids, const uint8_t *data,
-                                  const int64_t *offsets, const int64_t *ends, int32_t *flags,
+                                  const int64_t *offsets, const int64_t *ends,
+                                  const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
                                   int32_t *lens, int32_t *examined, void *workspace,
                                   size_t workspace_bytes, const gbfsm_plan *plan, void *stream) {
     if (n_tasks < 0 || n_automata < 0) return fail(GBFSM_INVALID_ARG, "negative task count");
@@ -245,7 +246,8 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
     if (max_words < 1) return fail(GBFSM_INVALID_ARG, "max_words must be >= 1");
     const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
     return launch_persistent(table, max_words, tasks, n_tasks, input_ids, data, offsets, ends,
-                             flags, lens, examined, workspace, workspace_bytes, p,
+                             chunks, chunk_records, flags, lens, examined, workspace,
+                             workspace_bytes, p,
                              static_cast<cudaStream_t>(stream));
 }
 

@@ -478,6 +478,74 @@ struct WarpNfa {
         return mode == kReg ? step_reg(sym) : step_general(sym);
     }
 
+    // Start from the set of records recs[rb .. re) (distinct states), closed under epsilon
+    // edges: the speculative superset of a chunk (first_edges of one byte).
+    __device__ int init_records(const gbfsm_edge *recs, uint32_t rb, uint32_t re) {
+        const uint32_t lane = lane_id();
+        const uint32_t cnt = re - rb;
+        if (cnt == 0) {
+            mode = kReg;
+            m = 0;
+            return kDead;
+        }
+        if (cnt <= 32u && S.C > 0) {
+            mine = (lane < cnt) ? load_edge<false>(recs + rb + lane) : make_uint4(0, 0, 0, 0);
+            const uint32_t eps = __ballot_sync(GBFSM_FULL_MASK, lane < cnt && (mine.y & GBFSM_EDGE_HAS_EPS));
+            const uint32_t acc = __ballot_sync(GBFSM_FULL_MASK, lane < cnt && (mine.y & GBFSM_EDGE_ACCEPT));
+            if (!(has_eps && eps)) {
+                mode = kReg;
+                m = (int)cnt;
+                return acc ? kAccept : kAlive;
+            }
+        }
+        uint32_t info_or = 0;
+        int n = walk_batch<false>(recs, lane == 0 ? rb : 0u, lane == 0 ? cnt : 0u, false, 0, S.V,
+                                  S.LB, 0, S.C, nullptr, info_or);
+        bool dense_now = n > S.C;
+        if (has_eps && (__reduce_or_sync(GBFSM_FULL_MASK, info_or) & GBFSM_EDGE_HAS_EPS)) {
+            if (!dense_now) n = sparse_closure<kStaged>(R, S.LB, n, S.C, S.V, info_or);
+            if (dense_now || n > S.C) {
+                __syncwarp();
+                n += dense_closure<kStaged>(R, W, S.V, S.FA, S.FB, info_or);
+                dense_now = true;
+            }
+        }
+        return finish_general(n, dense_now, info_or);
+    }
+
+    // Start from the states ids[0 .. count) (distinct, already closed under epsilon).
+    __device__ void init_ids(const uint32_t *ids, int count) {
+        const uint32_t lane = lane_id();
+        if (count <= 32) {
+            mine = ((int)lane < count) ? state_record(ids[lane]) : make_uint4(0, 0, 0, 0);
+            mode = kReg;
+            m = count;
+            return;
+        }
+        // more than a register list: rebuild through V (LB when it fits, else dense)
+        uint32_t info_or = 0;
+        for (int j = (int)lane; j < count; j += 32) {
+            const uint4 rec = state_record(ids[j]);
+            if (j < S.C) S.LB[j] = rec;
+            atomicOr(reinterpret_cast<unsigned long long *>(S.V + (rec.x >> 6)),
+                     1ull << (rec.x & 63u));
+        }
+        finish_general(count, count > S.C, info_or);
+    }
+
+    // Write the current members' ids to out[0 .. m) if there are at most `cap` of them
+    // and they are listed (REG or LIST); returns m, or -1 if not written.
+    __device__ int export_ids(uint32_t *out, int cap) const {
+        const uint32_t lane = lane_id();
+        if (m > cap || mode == kDense) return -1;
+        if (mode == kReg) {
+            if ((int)lane < m) out[lane] = mine.x;
+        } else {
+            for (int j = (int)lane; j < m; j += 32) out[j] = S.LA[j].x;
+        }
+        return m;
+    }
+
     // Leave V, D, FA and FB all-zero for the next input.
     __device__ void cleanup() {
         __syncwarp();

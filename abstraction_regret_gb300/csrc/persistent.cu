@@ -47,11 +47,202 @@ PersistLayout persist_layout(int32_t max_words, const gbfsm_plan &p) {
     return L;
 }
 
+// Outcome of one chunk (GBFSM_CHUNK_RECORD_BYTES bytes). Positions are byte counts from
+// the start of the chunk's input. For a speculative chunk the set sizes are recorded
+// after 1, 2, 4, ..., 32 bytes of the chunk; acc_after[c] is the first accepting position
+// strictly after checkpoint c (-1: none before the run stopped), dead_at the position at
+// which the (superset) run died. For an input's first chunk (exact) acc_after[0] /
+// dead_at are the input's own first accept / death. end_ids lists the set at the chunk
+// end when the run got there with at most kEndCap members (end_count, else -1).
+constexpr int kCheckpoints = 6;
+constexpr int kEndCap = 32;
+struct ChunkRecord {
+    int32_t counts[kCheckpoints];
+    int32_t acc_after[kCheckpoints];
+    int32_t dead_at;
+    int32_t end_count;
+    int32_t pad[2];
+    uint32_t end_ids[kEndCap];
+};
+static_assert(sizeof(ChunkRecord) == GBFSM_CHUNK_RECORD_BYTES, "chunk record layout");
+
+__device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }
+
+// CHUNK task: run one chunk (exactly when it is the input's first) and record it.
+__device__ void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
+                          const uint8_t *base, int64_t b, int64_t e, int index,
+                          ChunkRecord *rec) {
+    const uint32_t lane = lane_id();
+    WarpNfa<false> w(nfa, R, S);
+    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        counts[c] = 0;
+        acc_after[c] = -1;
+    }
+    int32_t dead_at = -1;
+    bool stopped = false;
+    int ev;
+    if (index == 0) {
+        ev = w.init_start();
+        if (ev == kAccept) {
+            acc_after[0] = 0;
+            stopped = true;
+        }
+    } else {
+        // superset of the true set after byte b-2, then one step on byte b-1
+        const uint32_t c0 = byte_at(base + b - 2);
+        ev = w.init_records(nfa.first_edges, __ldg(nfa.first_row + c0), __ldg(nfa.first_row + c0 + 1));
+        if (ev != kDead) ev = w.step(byte_at(base + b - 1));
+        if (ev == kDead) {
+            dead_at = (int32_t)b;
+            stopped = true;
+        }
+    }
+    // stream the chunk's bytes 16 at a time, one block ahead
+    const uint8_t *in = base + b;
+    const int64_t len = e - b;
+    const uint8_t *end = in + len;
+    const uint64_t addr = reinterpret_cast<uint64_t>(in);
+    const uint8_t *blk = reinterpret_cast<const uint8_t *>(addr & ~15ull);
+    int k = (int)(addr & 15ull);
+    uint4 chunk = make_uint4(0, 0, 0, 0), ahead = make_uint4(0, 0, 0, 0);
+    if (!stopped && len > 0) chunk = ld_stream16(blk);
+    if (!stopped && blk + 16 < end) ahead = ld_stream16(blk + 16);
+    int64_t j = 0;
+    while (!stopped && j < len) {
+        if (k == 16) {
+            blk += 16;
+            k = 0;
+            chunk = ahead;
+            if (blk + 16 < end) ahead = ld_stream16(blk + 16);
+        }
+        ev = w.step(byte_of(chunk, k));
+        ++k;
+        ++j;
+        const int32_t pos = (int32_t)(b + j);
+        if (index == 0) {
+            if (ev == kDead) {
+                dead_at = pos;
+                stopped = true;
+            } else if (ev == kAccept) {
+                acc_after[0] = pos;
+                stopped = true;
+            }
+            continue;
+        }
+        if (ev == kDead) {
+            dead_at = pos;
+            stopped = true;
+            break;
+        }
+        if (ev == kAccept) {
+#pragma unroll
+            for (int c = 0; c < kCheckpoints; ++c)
+                if (j > (1 << c) && acc_after[c] < 0) acc_after[c] = pos;
+            if (j > (1 << (kCheckpoints - 1))) stopped = true;  // first accept after the last checkpoint
+        }
+        if (j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) counts[31 - __clz((int)j)] = w.m;
+    }
+    int32_t end_count = -1;
+    if (!stopped) end_count = w.export_ids(rec->end_ids, kEndCap);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < kCheckpoints; ++c) {
+            rec->counts[c] = counts[c];
+            rec->acc_after[c] = acc_after[c];
+        }
+        rec->dead_at = dead_at;
+        rec->end_count = end_count;
+    }
+    w.cleanup();
+}
+
+// FIXUP task: resolve an input from its chunk records, re-running each chunk exactly only
+// until its exact set has as many members as the speculative superset at a checkpoint
+// (the superset contains the exact set, so equal sizes mean equal sets, and the rest of
+// the chunk is the recorded run).
+__device__ Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
+                             const uint8_t *base, int64_t len, const gbfsm_chunk *chunks,
+                             const ChunkRecord *recs, int first, int count, int64_t input_off) {
+    Verdict v{0, 0, len};
+    const ChunkRecord &r0 = recs[first];
+    if (r0.acc_after[0] >= 0) {
+        v.flag = 1;
+        v.len = r0.acc_after[0];
+        v.examined = r0.acc_after[0];
+        return v;
+    }
+    if (r0.dead_at >= 0) {
+        v.examined = r0.dead_at;
+        return v;
+    }
+    WarpNfa<false> w(nfa, R, S);
+    if (r0.end_count >= 0) {
+        w.init_ids(r0.end_ids, r0.end_count);
+    } else {  // the first chunk's end set was not recorded: recompute it exactly
+        w.init_start();
+        const int64_t e0 = chunks[first].end - input_off;
+        for (int64_t p = 0; p < e0; ++p) w.step(byte_at(base + p));
+    }
+    for (int k = 1; k < count; ++k) {
+        const gbfsm_chunk ch = chunks[first + k];
+        const ChunkRecord &rk = recs[first + k];
+        const int64_t b = ch.begin - input_off, e = ch.end - input_off;
+        int matched = -1;
+        int64_t j = 0;
+        while (b + j < e) {
+            const int ev = w.step(byte_at(base + b + j));
+            ++j;
+            if (ev == kDead) {
+                v.examined = b + j;
+                w.cleanup();
+                return v;
+            }
+            if (ev == kAccept) {
+                v.flag = 1;
+                v.len = (int32_t)(b + j);
+                v.examined = b + j;
+                w.cleanup();
+                return v;
+            }
+            if (matched < 0 && j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0 &&
+                w.m == rk.counts[31 - __clz((int)j)]) {
+                matched = 31 - __clz((int)j);
+                break;
+            }
+        }
+        if (matched >= 0) {
+            if (rk.acc_after[matched] >= 0) {
+                v.flag = 1;
+                v.len = rk.acc_after[matched];
+                v.examined = rk.acc_after[matched];
+                w.cleanup();
+                return v;
+            }
+            if (rk.dead_at >= 0) {
+                v.examined = rk.dead_at;
+                w.cleanup();
+                return v;
+            }
+            if (rk.end_count >= 0) {
+                w.cleanup();
+                w.init_ids(rk.end_ids, rk.end_count);
+            } else {
+                while (b + j < e) w.step(byte_at(base + b + j++));  // no event can occur here
+            }
+        }
+    }
+    w.cleanup();
+    return v;
+}
+
 __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
     const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
     int32_t n_tasks, const int32_t *__restrict__ input_ids, const uint8_t *__restrict__ data,
-    const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends, int32_t *flags,
-    int32_t *lens, int32_t *examined, PersistLayout L, uint32_t *ticket, uint8_t *gws) {
+    const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends,
+    const gbfsm_chunk *__restrict__ chunks, ChunkRecord *records, int32_t *flags, int32_t *lens,
+    int32_t *examined, PersistLayout L, uint32_t *ticket, uint8_t *gws) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int warp = (int)(threadIdx.x >> 5);
     const uint32_t lane = lane_id();
@@ -86,6 +277,28 @@ __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
             R.eps_row = nfa.eps_row;
             R.eps_edges = nfa.eps_edges;
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
+            if (task.kind == GBFSM_TASK_CHUNK) {
+                const gbfsm_chunk ch = chunks[task.first];
+                const int64_t off = offsets[ch.input];
+                if (S.C == 0) S.C = min(L.C, 32);  // speculation keeps small sets listed
+                run_chunk(nfa, R, S, data + off, ch.begin - off, ch.end - off, ch.index,
+                          records + task.first);
+                continue;
+            }
+            if (task.kind == GBFSM_TASK_FIXUP) {
+                const int32_t id = chunks[task.first].input;
+                const int64_t off = offsets[id];
+                const int64_t e = ends ? ends[id] : offsets[id + 1];
+                if (S.C == 0) S.C = min(L.C, 32);
+                const Verdict v = run_fixup(nfa, R, S, data + off, e - off, chunks, records,
+                                            task.first, task.count, off);
+                if (lane == 0) {
+                    flags[id] = v.flag;
+                    lens[id] = v.len;
+                    if (examined) examined[id] = (int32_t)v.examined;
+                }
+                continue;
+            }
             const int32_t id = input_ids[task.first];
             const int64_t b = offsets[id];
             const int64_t e = ends ? ends[id] : offsets[id + 1];
@@ -177,7 +390,8 @@ int32_t persistent_ctas_query(const PersistLayout &L, const gbfsm_plan &p) {
 gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
                                const uint8_t *data, const int64_t *offsets, const int64_t *ends,
-                               int32_t *flags, int32_t *lens, int32_t *examined, void *workspace,
+                               const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
+                               int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream) {
     const PersistLayout L = persist_layout(max_words, p);
     if (L.wpc < 1 || L.wpc * 32 > kMaxBlockThreads || (p.block_threads % 32) != 0)
@@ -200,8 +414,9 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
     const int needed = (n_tasks + L.wpc - 1) / L.wpc;
     if (grid > needed) grid = needed;
     persistent_kernel<<<grid, L.wpc * 32, smem, stream>>>(table, tasks, n_tasks, input_ids, data,
-                                                          offsets, ends, flags, lens, examined, L,
-                                                          ticket, gws);
+                                                          offsets, ends, chunks,
+                                                          static_cast<ChunkRecord *>(chunk_records),
+                                                          flags, lens, examined, L, ticket, gws);
     GBFSM_LAUNCH_CHECK("persistent_kernel launch");
     return GBFSM_OK;
 }

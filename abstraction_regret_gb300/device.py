@@ -52,6 +52,39 @@ def resolve_device(device=None) -> torch.device:
     return torch.device("cuda", d.index if d.index is not None else torch.cuda.current_device())
 
 
+SUPERSET_LIMIT = 1 << 25  # records; above this an automaton is not chunked speculatively
+
+
+def first_lists(nfa, limit: int = SUPERSET_LIMIT):
+    """Per byte c, the distinct targets of edges labelled c or ANY, as engine state records.
+
+    Returns ``(row int32[257], records uint32[k, 4])`` or ``None`` when the lists would
+    exceed ``limit`` records (many wildcard targets). After consuming byte c an NFA's
+    active set is contained in the epsilon closure of these targets, whatever the set
+    before it: the starting superset of a speculative chunk.
+    """
+    n = int(nfa.num_states)
+    syms = np.asarray(nfa.sym_symbols, dtype=np.int64)
+    tgts = np.asarray(nfa.sym_targets, dtype=np.int64)
+    any_t = np.unique(tgts[syms == ANY_SYMBOL])
+    plain = syms != ANY_SYMBOL
+    if int(plain.sum()) + 256 * any_t.size > limit:
+        return None
+    keys = syms[plain] * n + tgts[plain]
+    if any_t.size:
+        keys = np.concatenate([keys, (np.arange(256)[:, None] * n + any_t[None, :]).ravel()])
+    keys = np.unique(keys)
+    c, t = keys // n, keys % n
+    row = np.zeros(257, dtype=np.int64)
+    np.cumsum(np.bincount(c, minlength=256), out=row[1:])
+    srp = np.asarray(nfa.sym_row_ptr, dtype=np.int64)
+    erp = np.asarray(nfa.eps_row_ptr, dtype=np.int64)
+    acc = np.asarray(nfa.accept, dtype=bool)
+    info = (acc[t].astype(np.int64) << 9) | ((erp[t + 1] > erp[t]).astype(np.int64) << 10)
+    recs = np.stack([t, info, srp[t], srp[t + 1]], axis=1).astype(np.uint32)
+    return row.astype(np.int32), recs
+
+
 class DeviceNFA:
     """An NFA (ours or gpufsm's, duck-typed on the CSR fields) resident on a GPU."""
 
@@ -113,6 +146,18 @@ class DeviceNFA:
         d.accept_words = self.accept_words.data_ptr()
         d.num_sym_edges = nnz
         d.num_eps_edges = nne
+        lists = first_lists(nfa)
+        self.speculative = lists is not None
+        if lists is not None:
+            row, recs = lists
+            with torch.cuda.device(dev):
+                self.first_row = torch.from_numpy(np.ascontiguousarray(row)).to(dev)
+                self.first_edges = _padded(max(1, recs.shape[0]), 16, dev)
+                if recs.size:
+                    self.first_edges[: recs.nbytes].copy_(
+                        torch.from_numpy(np.ascontiguousarray(recs).view(np.uint8).ravel()))
+            d.first_row = self.first_row.data_ptr()
+            d.first_edges = self.first_edges.data_ptr()
         self.desc = d
 
     @property

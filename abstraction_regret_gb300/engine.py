@@ -1,17 +1,30 @@
-"""Persistent batched engine: many automata, many uneven inputs, one launch.
+"""Persistent batched engine: many automata, many uneven inputs, one resident launch.
 
 ``PersistentEngine`` keeps a pool of automata resident on the device (NFAs and DFAs of
 any size) together with a device table of their descriptors. A batch is a list of
-``(automaton index, input)`` requests; it becomes a task queue sorted longest first
-(NFA inputs one task each, DFA inputs grouped up to 32 per task for one lane each), and
-``gbfsm_persistent_run`` drains the queue with resident CTAs in a single launch.
+``(automaton index, input)`` requests. ``make_tasks`` turns it into a task queue sorted
+by estimated work, longest first:
 
-``GraphRunner`` captures one batch shape (host->device copies of the inputs and the
-task queue, the persistent launch, and the device->host copy of the verdicts) into a
-CUDA graph, so a repeated batch costs one graph launch.
+* DFA inputs are grouped up to 32 per task (one table walk per lane);
+* short NFA inputs are one task each (a warp per input);
+* long NFA inputs are cut into chunks that run **speculatively in parallel**: an
+  input's first chunk runs exactly from the start configuration; every later chunk
+  starts from a superset of the true active set (the targets of every edge labelled
+  with the byte two positions before the chunk, then one step) and records its set
+  sizes at checkpoints 1, 2, 4, ..., 32 bytes in, its first accept / death after each
+  checkpoint and its final set. A second launch of FIXUP tasks resolves each input
+  exactly: it re-runs a chunk from the true set only until the true set is as large as
+  the recorded superset at a checkpoint -- then they are equal, because the superset
+  always contains the true set and simulation preserves inclusion -- and continues
+  from the record. The verdicts are exactly those of a serial run.
 
-The reference has no counterpart: it builds one executor per call and launches once
-per automaton (src/gpufsm/api.py:27-52, backends/cuda/nfa.py:105-121).
+``gbfsm_persistent_run`` drains a queue with resident CTAs (one atomic ticket per task).
+``GraphRunner`` captures a whole batch (host->device copies, both launches, the
+device->host copy of the verdicts) in one CUDA graph.
+
+The reference has no counterpart: it builds one executor per call and launches once per
+automaton, one thread or warp per whole input (src/gpufsm/api.py:27-52,
+backends/cuda/nfa.py:105-121).
 """
 
 from __future__ import annotations
@@ -31,6 +44,7 @@ from .staging import Results, Staging
 
 DFA_GROUP = 32
 NFA_BYTE_WEIGHT = 4  # task-ordering weight of an NFA byte relative to a DFA byte
+MIN_CHUNK = 256      # shortest speculative chunk (bytes)
 
 
 @dataclass
@@ -39,13 +53,74 @@ class NfaChoice:
 
     technique: int = native.TECH_COMPACT  # TECH_COMPACT or TECH_WARP
     list_capacity: int = 128
+    speculate: bool = True                # allow chunked speculation for long inputs
+
+
+@dataclass
+class TaskPlan:
+    """Host-side task queue of one batch."""
+
+    tasks_a: np.ndarray    # int32 [na, 4]: WHOLE and CHUNK tasks (first launch)
+    tasks_b: np.ndarray    # int32 [nb, 4]: FIXUP tasks (second launch)
+    input_ids: np.ndarray  # int32 [n]
+    chunks: np.ndarray     # CHUNK_DTYPE [nc]
+    chunk_bytes: int
+
+
+class DeviceTasks:
+    """Pinned + device buffers for task plans, grown on demand and reused."""
+
+    def __init__(self, device) -> None:
+        self.device = device
+        self.cap_t = self.cap_i = self.cap_c = 0
+        self.na = self.nb = self.nc = 0
+
+    def _ensure(self, n_tasks: int, n_ids: int, n_chunks: int) -> None:
+        dev = self.device
+        if n_tasks > self.cap_t:
+            self.cap_t = max(n_tasks, 2 * self.cap_t, 256)
+            self.h_tasks = torch.empty(self.cap_t * 4, dtype=torch.int32, pin_memory=True)
+            self.d_tasks = torch.empty(self.cap_t * 4, dtype=torch.int32, device=dev)
+        if n_ids > self.cap_i:
+            self.cap_i = max(n_ids, 2 * self.cap_i, 256)
+            self.h_ids = torch.empty(self.cap_i, dtype=torch.int32, pin_memory=True)
+            self.d_ids = torch.empty(self.cap_i, dtype=torch.int32, device=dev)
+        if n_chunks > self.cap_c:
+            self.cap_c = max(n_chunks, 2 * self.cap_c, 64)
+            self.h_chunks = torch.empty(self.cap_c * 24, dtype=torch.uint8, pin_memory=True)
+            self.d_chunks = torch.empty(self.cap_c * 24, dtype=torch.uint8, device=dev)
+            self.d_records = torch.empty(self.cap_c * native.CHUNK_RECORD_BYTES,
+                                         dtype=torch.uint8, device=dev)
+
+    def upload(self, plan: TaskPlan, stream) -> None:
+        """Copy a plan into the pinned buffers and enqueue its host->device copies."""
+        na, nb = plan.tasks_a.shape[0], plan.tasks_b.shape[0]
+        nc = plan.chunks.shape[0]
+        self._ensure(na + nb + 1, plan.input_ids.size + 1, nc + 1)
+        if na:
+            self.h_tasks.numpy()[: na * 4] = plan.tasks_a.reshape(-1)
+        if nb:
+            self.h_tasks.numpy()[na * 4:(na + nb) * 4] = plan.tasks_b.reshape(-1)
+        self.h_ids.numpy()[: plan.input_ids.size] = plan.input_ids
+        if nc:
+            self.h_chunks.numpy()[: nc * 24] = plan.chunks.view(np.uint8)
+        with torch.cuda.stream(stream):
+            nt = max(1, na + nb) * 4
+            self.d_tasks[:nt].copy_(self.h_tasks[:nt], non_blocking=True)
+            ni = max(1, plan.input_ids.size)
+            self.d_ids[:ni].copy_(self.h_ids[:ni], non_blocking=True)
+            if nc:
+                self.d_chunks[: nc * 24].copy_(self.h_chunks[: nc * 24], non_blocking=True)
+        self.na, self.nb, self.nc = na, nb, nc
 
 
 class PersistentEngine:
     """A resident automaton pool plus the persistent launch over it."""
 
     def __init__(self, automata, device=None, choices=None, block_threads: int = 256,
-                 list_capacity: int | None = None, ctas_per_sm: int = 0) -> None:
+                 list_capacity: int | None = None, ctas_per_sm: int = 0,
+                 chunk_bytes: int | None = 0) -> None:
+        """``chunk_bytes``: 0 = chosen per batch, None = never chunk, else a fixed size."""
         self.device = resolve_device(device)
         self.automata = list(automata)
         if not self.automata:
@@ -56,6 +131,9 @@ class PersistentEngine:
             self.dev.append(DeviceNFA(a, self.device) if k is Kind.NFA else DeviceDFA(a, self.device))
         choices = list(choices) if choices is not None else [NfaChoice() for _ in self.automata]
         self.choices = choices
+        self.chunk_bytes = chunk_bytes
+        self.can_chunk = np.array([k is Kind.NFA and d.speculative and c.speculate
+                                   for k, d, c in zip(self.kinds, self.dev, choices)], dtype=bool)
         caps = [c.list_capacity for c, k in zip(choices, self.kinds) if k is Kind.NFA]
         cap = list_capacity if list_capacity else (max(caps) if caps else 32)
         self.max_words = max([d.num_words for d in self.dev if isinstance(d, DeviceNFA)] or [1])
@@ -84,50 +162,99 @@ class PersistentEngine:
                     table[i].dfa = d.desc
             raw = np.frombuffer(bytes(table), dtype=np.uint8).copy()
             self.table = torch.from_numpy(raw).to(self.device)
+            props = torch.cuda.get_device_properties(self.device)
+        self.resident_warps = props.multi_processor_count * self.ctas_per_sm * (block_threads // 32)
         self._staging = Staging(self.device)
         self._results = Results(self.device)
-        self._task_cap = 0
+        self._tasks = DeviceTasks(self.device)
 
     # ---- task queue ---------------------------------------------------------------------
 
-    def make_tasks(self, aut_ids: np.ndarray, lengths: np.ndarray):
-        """Task queue (int32 ``[n_tasks, 4]``) and input-id list, most work first.
+    def auto_chunk_bytes(self, nfa_bytes: int) -> int:
+        """Chunk size giving each resident warp about four chunks of the NFA bytes."""
+        per = nfa_bytes // max(1, 4 * self.resident_warps)
+        size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
+        return int(min(size, 1 << 20))
 
-        NFA inputs are one task each; a DFA's inputs are sorted longest first and grouped
-        32 to a task (one per lane). Tasks are ordered by estimated cost (bytes, with an
-        NFA byte weighted ``NFA_BYTE_WEIGHT`` DFA bytes) so the longest serial chains
-        start first.
-        """
+    def make_tasks(self, aut_ids, lengths, starts=None) -> TaskPlan:
+        """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
+        packed back to back from 0) on automaton ``aut_ids[i]``."""
         aut_ids = np.asarray(aut_ids, dtype=np.int64)
         lengths = np.asarray(lengths, dtype=np.int64)
         n = aut_ids.size
+        empty = np.zeros((0, 4), dtype=np.int32)
+        no_chunks = np.zeros(0, dtype=native.CHUNK_DTYPE)
         if n == 0:
-            return np.zeros((0, 4), dtype=np.int32), np.zeros(1, dtype=np.int32)
+            return TaskPlan(empty, empty, np.zeros(1, np.int32), no_chunks, 0)
         if aut_ids.min() < 0 or aut_ids.max() >= len(self.automata):
             raise ValueError("request names an automaton outside the pool")
+        if starts is None:
+            starts = np.zeros(n, dtype=np.int64)
+            np.cumsum(lengths[:-1], out=starts[1:])
+        starts = np.asarray(starts, dtype=np.int64)
         is_dfa = np.array([k is Kind.DFA for k in self.kinds], dtype=bool)[aut_ids]
         nfa_idx = np.flatnonzero(~is_dfa)
         dfa_idx = np.flatnonzero(is_dfa)
         dfa_idx = dfa_idx[np.lexsort((-lengths[dfa_idx], aut_ids[dfa_idx]))]
         input_ids = np.concatenate([nfa_idx, dfa_idx]).astype(np.int32)
-        rows = [np.stack([aut_ids[nfa_idx], np.arange(nfa_idx.size), np.ones_like(nfa_idx),
-                          lengths[nfa_idx] * NFA_BYTE_WEIGHT], axis=1)]
+        rows = []
+        # NFA inputs: whole, or chunked when long and the automaton allows speculation
+        chunk = 0
+        if self.chunk_bytes is not None and nfa_idx.size:
+            chunk = self.chunk_bytes or self.auto_chunk_bytes(int(lengths[nfa_idx].sum()))
+            chunk = max(int(chunk), MIN_CHUNK)
+        split = np.zeros(n, dtype=bool)
+        if chunk:
+            split[nfa_idx] = (lengths[nfa_idx] >= 2 * chunk) & self.can_chunk[aut_ids[nfa_idx]]
+        whole = nfa_idx[~split[nfa_idx]]
+        pos_of = np.empty(n, dtype=np.int64)
+        pos_of[nfa_idx] = np.arange(nfa_idx.size)
+        rows.append(np.stack([aut_ids[whole], pos_of[whole], np.ones_like(whole),
+                              np.full_like(whole, native.TASK_WHOLE),
+                              lengths[whole] * NFA_BYTE_WEIGHT], axis=1))
+        chunk_list, fix_rows = [], []
+        if split.any():
+            sidx = np.flatnonzero(split)
+            counts = lengths[sidx] // chunk  # the last chunk absorbs the remainder
+            first = np.zeros(sidx.size, dtype=np.int64)
+            np.cumsum(counts[:-1], out=first[1:])
+            total = int(counts.sum())
+            ch = np.zeros(total, dtype=native.CHUNK_DTYPE)
+            inp = np.repeat(sidx, counts)
+            idx = np.arange(total) - np.repeat(first, counts)
+            ch["input"] = inp
+            ch["index"] = idx
+            ch["begin"] = starts[inp] + idx * chunk
+            last = idx == np.repeat(counts - 1, counts)
+            ch["end"] = np.where(last, starts[inp] + lengths[inp], ch["begin"] + chunk)
+            chunk_list.append(ch)
+            rows.append(np.stack([aut_ids[inp], np.arange(total), np.ones(total, np.int64),
+                                  np.full(total, native.TASK_CHUNK),
+                                  (ch["end"] - ch["begin"]) * NFA_BYTE_WEIGHT], axis=1))
+            fix_rows.append(np.stack([aut_ids[sidx], first, counts,
+                                      np.full(sidx.size, native.TASK_FIXUP), counts], axis=1))
         if dfa_idx.size:
             sa = aut_ids[dfa_idx]
             seg_starts = np.flatnonzero(np.r_[True, sa[1:] != sa[:-1]])
             seg_ends = np.r_[seg_starts[1:], sa.size]
-            firsts, counts = [], []
+            firsts, cnts = [], []
             for s, e in zip(seg_starts.tolist(), seg_ends.tolist()):
                 for gs in range(s, e, DFA_GROUP):
                     firsts.append(gs)
-                    counts.append(min(DFA_GROUP, e - gs))
+                    cnts.append(min(DFA_GROUP, e - gs))
             g = np.asarray(firsts, dtype=np.int64)
-            rows.append(np.stack([sa[g], nfa_idx.size + g, np.asarray(counts, dtype=np.int64),
-                                  lengths[dfa_idx[g]]], axis=1))
+            rows.append(np.stack([sa[g], nfa_idx.size + g, np.asarray(cnts, dtype=np.int64),
+                                  np.full(g.size, native.TASK_WHOLE), lengths[dfa_idx[g]]], axis=1))
         t = np.concatenate(rows)
-        t = t[np.argsort(-t[:, 3], kind="stable")]
-        t[:, 3] = 0
-        return t.astype(np.int32), input_ids
+        t = t[np.argsort(-t[:, 4], kind="stable")][:, :4]
+        if fix_rows:
+            f = np.concatenate(fix_rows)
+            f = f[np.argsort(-f[:, 4], kind="stable")][:, :4]
+        else:
+            f = empty
+        chunks = np.concatenate(chunk_list) if chunk_list else no_chunks
+        return TaskPlan(np.ascontiguousarray(t, dtype=np.int32),
+                        np.ascontiguousarray(f, dtype=np.int32), input_ids, chunks, chunk)
 
     # ---- launches -------------------------------------------------------------------------
 
@@ -135,42 +262,36 @@ class PersistentEngine:
         """A separate workspace (queue ticket + dense scratch) for a concurrent launch."""
         return torch.zeros(self.ws_bytes, dtype=torch.uint8, device=self.device)
 
-    def launch(self, d_data, d_off, d_tasks, n_tasks, d_ids, d_flags, d_lens, d_examined=None,
-               stream=None, d_ends=None, workspace=None) -> None:
-        """Enqueue the persistent launch (no synchronisation).
-
-        ``d_data`` is a device tensor or a raw address (e.g. of pinned host memory the
-        device reads directly); with ``d_ends`` input i spans ``[d_off[i], d_ends[i])``.
-        """
-        stream = stream or torch.cuda.current_stream(self.device)
-        ws = self.workspace if workspace is None else workspace
-        data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
+    def _run(self, tasks_ptr, n_tasks, dt: DeviceTasks, data_ptr, d_off, d_ends, d_flags, d_lens,
+             d_examined, ws, stream) -> None:
         st = native.lib().gbfsm_persistent_run(
-            self.table.data_ptr(), len(self.automata), self.max_words, d_tasks.data_ptr(),
-            int(n_tasks), d_ids.data_ptr(), data_ptr, d_off.data_ptr(),
+            self.table.data_ptr(), len(self.automata), self.max_words, tasks_ptr, int(n_tasks),
+            dt.d_ids.data_ptr(), data_ptr, d_off.data_ptr(),
             d_ends.data_ptr() if d_ends is not None else None,
+            dt.d_chunks.data_ptr() if dt.nc else None,
+            dt.d_records.data_ptr() if dt.nc else None,
             d_flags.data_ptr(), d_lens.data_ptr(),
             d_examined.data_ptr() if d_examined is not None else None,
             ws.data_ptr(), self.ws_bytes, ctypes.byref(self.plan), stream.cuda_stream)
         native.check(st, "gbfsm_persistent_run")
 
-    def _upload_tasks(self, tasks: np.ndarray, ids: np.ndarray, stream):
-        need_t = max(1, tasks.shape[0]) * 4
-        need_i = max(1, ids.size)
-        if need_t > self._task_cap or need_i > getattr(self, "_id_cap", 0):
-            self._task_cap = max(need_t, 2 * self._task_cap)
-            self._id_cap = max(need_i, 2 * getattr(self, "_id_cap", 0))
-            self._h_tasks = torch.empty(self._task_cap, dtype=torch.int32, pin_memory=True)
-            self._d_tasks = torch.empty(self._task_cap, dtype=torch.int32, device=self.device)
-            self._h_ids = torch.empty(self._id_cap, dtype=torch.int32, pin_memory=True)
-            self._d_ids = torch.empty(self._id_cap, dtype=torch.int32, device=self.device)
-        nt = tasks.size
-        self._h_tasks.numpy()[:nt] = tasks.reshape(-1)
-        self._h_ids.numpy()[:ids.size] = ids
-        with torch.cuda.stream(stream):
-            self._d_tasks[:max(nt, 1)].copy_(self._h_tasks[:max(nt, 1)], non_blocking=True)
-            self._d_ids[:ids.size].copy_(self._h_ids[:ids.size], non_blocking=True)
-        return self._d_tasks, self._d_ids
+    def launch(self, d_data, d_off, dt: DeviceTasks, d_flags, d_lens, d_examined=None,
+               stream=None, d_ends=None, workspace=None) -> int:
+        """Enqueue the batch's launches (one, or two with speculative chunks); returns how
+        many kernels were launched. ``d_data`` is a device tensor or a raw device address
+        (e.g. of pinned host memory read in place); with ``d_ends`` input i spans
+        ``[d_off[i], d_ends[i])``."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        ws = self.workspace if workspace is None else workspace
+        data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
+        base = dt.d_tasks.data_ptr()
+        self._run(base, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens, d_examined, ws,
+                  stream)
+        if dt.nb:
+            self._run(base + dt.na * 16, dt.nb, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
+                      d_examined, ws, stream)
+            return 2
+        return 1
 
     def run_requests(self, aut_ids, inputs, with_examined: bool = False):
         """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``.
@@ -182,15 +303,15 @@ class PersistentEngine:
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
         lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
-        tasks, ids = self.make_tasks(np.asarray(aut_ids), lengths)
+        plan = self.make_tasks(np.asarray(aut_ids), lengths)
         d_data, d_off, _, _ = self._staging.put(inputs, stream)
-        d_tasks, d_ids = self._upload_tasks(tasks, ids, stream)
+        self._tasks.upload(plan, stream)
         self._results.ensure(max(n, 1))
         res = self._results
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        self.launch(d_data, d_off, d_tasks, tasks.shape[0], d_ids, res.d[0], res.d[1],
+        self.launch(d_data, d_off, self._tasks, res.d[0], res.d[1],
                     res.d[2] if with_examined else None, stream)
         e1.record(stream)
         res.fetch(n, stream)
@@ -216,11 +337,10 @@ class PersistentEngine:
 
 
 class GraphRunner:
-    """A fixed batch captured as one CUDA graph: H2D inputs, persistent launch, D2H verdicts.
+    """A fixed batch captured as one CUDA graph: H2D inputs, the launches, D2H verdicts.
 
     The batch (flat uint8 data + int64 offsets + automaton ids) is fixed at construction;
-    ``replay`` re-runs it end to end. ``set_inputs`` may rewrite the pinned input bytes
-    in place (same lengths) between replays.
+    ``replay`` re-runs it end to end.
     """
 
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
@@ -230,28 +350,26 @@ class GraphRunner:
         n = len(offsets) - 1
         self.n = n
         lengths = np.diff(np.asarray(offsets, dtype=np.int64))
-        tasks, ids = engine.make_tasks(np.asarray(aut_ids), lengths)
-        self.n_tasks = tasks.shape[0]
+        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths)
         total = int(offsets[-1])
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
         self.h_data.numpy()[:total] = np.asarray(data[:total], dtype=np.uint8)
         self.h_off = torch.from_numpy(np.asarray(offsets, dtype=np.int64).copy()).pin_memory()
-        self.h_tasks = torch.from_numpy(tasks.reshape(-1).copy() if tasks.size else
-                                        np.zeros(4, np.int32)).pin_memory()
-        self.h_ids = torch.from_numpy(ids.copy()).pin_memory()
         self.h_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, pin_memory=True)
         self.d_data = torch.empty_like(self.h_data, device=dev)
         self.d_off = torch.empty_like(self.h_off, device=dev)
-        self.d_tasks = torch.empty_like(self.h_tasks, device=dev)
-        self.d_ids = torch.empty_like(self.h_ids, device=dev)
         self.d_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, device=dev)
+        self.tasks = DeviceTasks(dev)
         self.with_examined = with_examined
-        self.h2d_bytes = padded + self.h_off.numel() * 8 + self.h_tasks.numel() * 4 + \
-            self.h_ids.numel() * 4
-        self.d2h_bytes = self.h_out.numel() * 4
         self.stream = torch.cuda.Stream(dev)
-        # warm-up outside capture (sets kernel attributes, loads modules)
+        p = self.task_plan
+        self.h2d_bytes = padded + self.h_off.numel() * 8 + (p.tasks_a.shape[0] +
+                                                             p.tasks_b.shape[0]) * 16 + \
+            p.input_ids.size * 4 + p.chunks.shape[0] * 24
+        self.d2h_bytes = self.h_out.numel() * 4
+        self.launches_per_step = 0
+        # warm-up outside capture (kernel attributes, occupancy queries, module load)
         with torch.cuda.stream(self.stream):
             self._body()
         self.stream.synchronize()
@@ -264,23 +382,22 @@ class GraphRunner:
         s = torch.cuda.current_stream(self.engine.device)
         self.d_data.copy_(self.h_data, non_blocking=True)
         self.d_off.copy_(self.h_off, non_blocking=True)
-        self.d_tasks.copy_(self.h_tasks, non_blocking=True)
-        self.d_ids.copy_(self.h_ids, non_blocking=True)
-        self.engine.launch(self.d_data, self.d_off, self.d_tasks, self.n_tasks, self.d_ids,
-                           self.d_out[0], self.d_out[1],
-                           self.d_out[2] if self.with_examined else None, s)
+        self.tasks.upload(self.task_plan, s)
+        self.launches_per_step = self.engine.launch(
+            self.d_data, self.d_off, self.tasks, self.d_out[0], self.d_out[1],
+            self.d_out[2] if self.with_examined else None, s)
         self.h_out.copy_(self.d_out, non_blocking=True)
 
-    def replay(self, stream=None) -> None:
+    def replay(self) -> None:
         """Launch the captured graph (asynchronous)."""
         self.graph.replay()
 
-    def kernel_only(self, stream=None) -> None:
-        """The persistent launch alone on resident inputs (for device-side timing)."""
+    def kernel_only(self, stream=None) -> int:
+        """The launches alone on resident inputs (for device-side timing)."""
         stream = stream or torch.cuda.current_stream(self.engine.device)
-        self.engine.launch(self.d_data, self.d_off, self.d_tasks, self.n_tasks, self.d_ids,
-                           self.d_out[0], self.d_out[1],
-                           self.d_out[2] if self.with_examined else None, stream)
+        return self.engine.launch(self.d_data, self.d_off, self.tasks, self.d_out[0],
+                                  self.d_out[1], self.d_out[2] if self.with_examined else None,
+                                  stream)
 
     def verdicts(self):
         h = self.h_out.numpy()

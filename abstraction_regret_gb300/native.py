@@ -50,6 +50,8 @@ class NfaDev(ctypes.Structure):
         ("accept_words", ctypes.c_void_p),
         ("num_sym_edges", ctypes.c_uint64),
         ("num_eps_edges", ctypes.c_uint64),
+        ("first_row", ctypes.c_void_p),
+        ("first_edges", ctypes.c_void_p),
     ]
 
 
@@ -89,7 +91,17 @@ class Automaton(ctypes.Structure):
 
 class Task(ctypes.Structure):
     _fields_ = [("automaton", ctypes.c_int32), ("first", ctypes.c_int32),
-                ("count", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("count", ctypes.c_int32), ("kind", ctypes.c_int32)]
+
+
+class Chunk(ctypes.Structure):
+    _fields_ = [("input", ctypes.c_int32), ("index", ctypes.c_int32),
+                ("begin", ctypes.c_int64), ("end", ctypes.c_int64)]
+
+
+TASK_WHOLE, TASK_CHUNK, TASK_FIXUP = 0, 1, 2
+CHUNK_RECORD_BYTES = 192
+CHUNK_DTYPE = [("input", "<i4"), ("index", "<i4"), ("begin", "<i8"), ("end", "<i8")]
 
 
 _vp = ctypes.c_void_p
@@ -113,7 +125,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_persistent_workspace_bytes": (_sz, [_i32, _P(Plan)]),
     "gbfsm_persistent_ctas_per_sm": (_i32, [_i32, _P(Plan)]),
     "gbfsm_persistent_run": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
-                                            _vp, _vp, _vp, _sz, _P(Plan), _vp]),
+                                            _vp, _vp, _vp, _vp, _vp, _sz, _P(Plan), _vp]),
     "gbfsm_run_multistream": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_shared": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_async": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),

@@ -37,7 +37,7 @@ import numpy as np
 import torch
 
 from . import native
-from .engine import PersistentEngine
+from .engine import DeviceTasks, PersistentEngine
 from .packing import PAD
 from .registry import Kind
 
@@ -83,10 +83,7 @@ class _Slot:
             self.d_data = torch.empty(batch_bytes + PAD, dtype=torch.uint8, device=dev)
         self.h_off = torch.empty(2 * max_requests + 1, dtype=torch.int64, pin_memory=True)
         self.d_off = torch.empty(2 * max_requests + 1, dtype=torch.int64, device=dev)
-        self.h_tasks = torch.empty(4 * max_requests, dtype=torch.int32, pin_memory=True)
-        self.d_tasks = torch.empty(4 * max_requests, dtype=torch.int32, device=dev)
-        self.h_ids = torch.empty(max_requests, dtype=torch.int32, pin_memory=True)
-        self.d_ids = torch.empty(max_requests, dtype=torch.int32, device=dev)
+        self.tasks = DeviceTasks(dev)
         self.h_out = torch.zeros((2, max_requests), dtype=torch.int32, pin_memory=True)
         self.d_out = torch.zeros((2, max_requests), dtype=torch.int32, device=dev)
         self.reqs: list[int] = []
@@ -120,8 +117,7 @@ class Server:
         n = len(reqs)
         a = aut_ids[reqs]
         ln = lengths[reqs]
-        tasks, ids = self.engine.make_tasks(a, ln)
-        nt = tasks.shape[0]
+        plan = self.engine.make_tasks(a, ln, starts[reqs] if self.zero_copy else None)
         if self.zero_copy:
             off = slot.h_off.numpy()
             off[:n] = starts[reqs]
@@ -137,8 +133,6 @@ class Server:
                 h[pos:pos + k] = pool[s:s + k]
                 pos += k
             h[pos:pos + PAD] = 0
-        slot.h_tasks.numpy()[:nt * 4] = tasks.reshape(-1)
-        slot.h_ids.numpy()[:n] = ids
         with torch.cuda.stream(slot.stream):
             if self.zero_copy:
                 slot.d_off[:2 * n].copy_(slot.h_off[:2 * n], non_blocking=True)
@@ -150,11 +144,9 @@ class Server:
                 slot.d_data[:used].copy_(slot.h_data[:used], non_blocking=True)
                 slot.d_off[:n + 1].copy_(slot.h_off[:n + 1], non_blocking=True)
                 d_off, d_ends, data = slot.d_off, None, slot.d_data
-            slot.d_tasks[:max(nt, 1) * 4].copy_(slot.h_tasks[:max(nt, 1) * 4], non_blocking=True)
-            slot.d_ids[:n].copy_(slot.h_ids[:n], non_blocking=True)
-            self.engine.launch(data, d_off, slot.d_tasks, nt, slot.d_ids, slot.d_out[0],
-                               slot.d_out[1], None, slot.stream, d_ends=d_ends,
-                               workspace=slot.workspace)
+            slot.tasks.upload(plan, slot.stream)
+            self.engine.launch(data, d_off, slot.tasks, slot.d_out[0], slot.d_out[1], None,
+                               slot.stream, d_ends=d_ends, workspace=slot.workspace)
             for r in range(2):
                 slot.h_out[r, :n].copy_(slot.d_out[r, :n], non_blocking=True)
             slot.event.record(slot.stream)

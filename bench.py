@@ -269,6 +269,7 @@ def main(argv=None) -> int:
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             ms = time_launches(runner.kernel_only, stream, args.steps, args.warmup)
+        launches = runner.launches_per_step * args.steps
         torch.cuda.synchronize()
     barrier()
     if world > 1:
@@ -376,8 +377,10 @@ def main(argv=None) -> int:
                            "offered_bytes": offered, "examined_bytes": examined_bytes,
                            "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}",
-                           "technique": "persistent (autotuned per automaton)"},
-                "e2e": e2e, "gpu_launches": args.steps, "oracle_gate": gate,
+                           "technique": "persistent, speculative chunks of "
+                                        f"{runner.task_plan.chunk_bytes} B "
+                                        f"({runner.task_plan.chunks.shape[0]} chunks)"},
+                "e2e": e2e, "gpu_launches": launches, "oracle_gate": gate,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
         line.update(extras)
         print(json.dumps(line), flush=True)

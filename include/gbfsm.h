@@ -87,6 +87,13 @@ typedef struct gbfsm_nfa_dev {
     const uint64_t *accept_words;   /* [num_words], pack_accept layout */
     uint64_t num_sym_edges;
     uint64_t num_eps_edges;
+    /* Optional (NULL = no speculative chunking for this automaton): for each byte c, the
+     * distinct targets of all edges labelled c or ANY, as state records
+     * first_edges[first_row[c] .. first_row[c+1]) (first_row has 257 entries). After any
+     * byte c the active set is contained in the epsilon closure of these targets, which
+     * makes them a safe starting superset for a chunk that begins mid-input. */
+    const uint32_t *first_row;
+    const gbfsm_edge *first_edges;
 } gbfsm_nfa_dev;
 
 /* A DFA on the device. table[s * 256 + c] holds the successor of s on byte c in the low
@@ -195,20 +202,43 @@ typedef struct gbfsm_automaton {
     gbfsm_dfa_dev dfa;     /* valid when kind == 1 */
 } gbfsm_automaton;
 
-/* One task: `count` inputs of automaton `automaton`, whose input indices are
- * input_ids[first .. first + count). An NFA task has count 1 (a warp runs it); a DFA
- * task has 1..32 inputs (one lane each). */
+/* One task. kind GBFSM_TASK_WHOLE: `count` inputs of automaton `automaton`, whose input
+ * indices are input_ids[first .. first + count); an NFA task has count 1 (a warp runs it),
+ * a DFA task 1..32 inputs (one lane each). kind GBFSM_TASK_CHUNK: chunk `first` of the
+ * chunk table, simulated speculatively (or exactly when it is an input's first chunk);
+ * its outcome goes to the chunk records. kind GBFSM_TASK_FIXUP: input whose chunks are
+ * chunks[first .. first + count), resolved exactly from the chunk records of an earlier
+ * launch; writes the input's verdict. */
 typedef struct gbfsm_task {
     int32_t automaton;
     int32_t first;
     int32_t count;
-    int32_t reserved;
+    int32_t kind;
 } gbfsm_task;
+
+#define GBFSM_TASK_WHOLE 0
+#define GBFSM_TASK_CHUNK 1
+#define GBFSM_TASK_FIXUP 2
+
+/* A piece of an NFA input: bytes data[begin .. end) of input `input`; `index` counts the
+ * input's chunks from 0. Chunks after the first must start at least 2 bytes into the
+ * input and span at least 32 bytes. */
+typedef struct gbfsm_chunk {
+    int32_t input;
+    int32_t index;
+    int64_t begin;
+    int64_t end;
+} gbfsm_chunk;
+
+/* Bytes of one chunk record (device scratch written by CHUNK tasks, read by FIXUP). */
+#define GBFSM_CHUNK_RECORD_BYTES 192
 
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan);
 
-/* Run `n_tasks` tasks. table/tasks/input_ids are device arrays. Input i is
+/* Run `n_tasks` tasks. table/tasks/input_ids (and chunks/chunk_records, needed only by
+ * CHUNK and FIXUP tasks) are device arrays. Speculative chunking takes two calls on one
+ * stream: the CHUNK tasks (with any WHOLE tasks), then the FIXUP tasks. Input i is
  * data[offsets[i] .. ends[i]) when `ends` is non-NULL (spans anywhere in `data`, e.g.
  * requests left in place in a pinned host pool that the device reads directly), else
  * data[offsets[i] .. offsets[i+1]). Results are written by input index. workspace
@@ -218,7 +248,8 @@ size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *pla
 gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automata,
                                   int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
                                   const int32_t *input_ids, const uint8_t *data,
-                                  const int64_t *offsets, const int64_t *ends, int32_t *flags,
+                                  const int64_t *offsets, const int64_t *ends,
+                                  const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
                                   int32_t *lens, int32_t *examined, void *workspace,
                                   size_t workspace_bytes, const gbfsm_plan *plan, void *stream);
 

@@ -239,3 +239,53 @@ def test_c4_all_pairs_one_launch(variant):
     b = W.c4(variant)
     assert b.n_inputs == 1024
     _check_batch(b, _persistent)
+
+
+# ---- speculative chunking in the persistent engine ------------------------------------
+
+@pytest.mark.parametrize("chunk", [256, 1000, 4096])
+def test_chunked_persistent_matches_oracle_on_live_walks(chunk):
+    b = W.c1("live")
+    for a in (b.automata[0], W.without_accepts(b.automata[0])):
+        eng = PersistentEngine([a], chunk_bytes=chunk)
+        plan = eng.make_tasks(np.zeros(b.n_inputs, np.int64), np.diff(b.offsets))
+        assert plan.tasks_b.shape[0] == (b.n_inputs if chunk <= 2048 else 0)
+        f, l, e, _, _ = eng.run_requests(np.zeros(b.n_inputs), b.inputs(), with_examined=True)
+        of, ol, oe, _ = O.nfa_batch(a, b.data, b.offsets)
+        assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
+
+
+def test_chunked_persistent_with_epsilon_and_wildcards():
+    import random
+
+    rng = random.Random(5)
+    automata, reqs = [], []
+    for k in range(12):
+        b = G.NFABuilder()
+        n = rng.randint(2, 300)
+        for _ in range(n):
+            b.add_state(accept=rng.random() < 0.004)
+        b.set_start(rng.randrange(n))
+        for s in range(n):
+            for _ in range(rng.randint(1, 4)):
+                sym = G.ANY_SYMBOL if rng.random() < 0.03 else ord(rng.choice("abcd"))
+                b.add_transition(s, sym, rng.randrange(n))
+            for _ in range(rng.randint(0, 1)):
+                b.add_epsilon(s, rng.randrange(n))
+        automata.append(b.build())
+        for _ in range(6):
+            reqs.append((k, bytes(ord(rng.choice("abcd")) for _ in range(rng.randint(0, 3000)))))
+    for chunk in (256, 700):
+        eng = PersistentEngine(automata, chunk_bytes=chunk)
+        f, l, _, _, _ = eng.run_requests([a for a, _ in reqs], [d for _, d in reqs])
+        want = [O.simulate(automata[a], d) for a, d in reqs]
+        assert list(zip(f.astype(bool).tolist(), l.tolist())) == want, chunk
+
+
+@pytest.mark.parametrize("variant", ["live", "sustained"])
+def test_c3_chunked_small_chunks(variant):
+    b = W.c3(variant, n_inputs=256)
+    eng = PersistentEngine(b.automata, chunk_bytes=512)
+    f, l, e, _, _ = eng.run_requests(b.aut_ids, b.inputs(), with_examined=True)
+    of, ol, oe, _ = O.nfa_batch(b.automata[0], b.data, b.offsets)
+    assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)

@@ -1,0 +1,162 @@
+"""The speculative chunk protocol, checked on the CPU with a set-based model.
+
+``run_chunk`` / ``run_fixup`` below restate the device protocol of the persistent
+engine (csrc/persistent.cu) with Python sets: a chunk after the first starts from the
+epsilon closure of every target of an edge labelled with the byte two positions before
+it, steps over the byte just before it, records its set sizes after 1, 2, 4, ..., 32
+bytes, the first accept after each checkpoint and where it died; the fix-up re-runs each
+chunk exactly until the exact set is as large as the superset at a checkpoint. The
+model must give the oracle's verdict on every input, for any chunk size -- this pins the
+protocol itself, independently of the kernels (the GPU tests pin the kernels against
+the oracle).
+"""
+
+from __future__ import annotations
+
+import random
+
+import numpy as np
+import pytest
+
+from abstraction_regret_gb300 import ANY_SYMBOL, NFABuilder
+from abstraction_regret_gb300 import workloads as W
+from abstraction_regret_gb300.device import first_lists
+from oracle.oracle import epsilon_closure, simulate
+
+CHECKPOINTS = 6
+
+
+def step(nfa, cur, b):
+    rp, tg, sy = nfa.sym_row_ptr, nfa.sym_targets, nfa.sym_symbols
+    nxt = set()
+    for s in cur:
+        for k in range(int(rp[s]), int(rp[s + 1])):
+            if int(sy[k]) in (b, ANY_SYMBOL):
+                nxt.add(int(tg[k]))
+    return epsilon_closure(nxt, nfa) if nxt else set()
+
+
+def accepts(nfa, cur):
+    return any(nfa.accept[s] for s in cur)
+
+
+def run_chunk(nfa, data, b, e, index, lists):
+    rec = {"counts": [0] * CHECKPOINTS, "acc_after": [-1] * CHECKPOINTS, "dead_at": -1,
+           "end": None}
+    if index == 0:
+        cur = epsilon_closure({int(nfa.start_state)}, nfa)
+        if accepts(nfa, cur):
+            rec["acc_after"][0] = 0
+            return rec
+    else:
+        row, recs = lists
+        c0 = data[b - 2]
+        cur = epsilon_closure({int(t) for t in recs[row[c0]:row[c0 + 1], 0]}, nfa)
+        cur = step(nfa, cur, data[b - 1]) if cur else set()
+        if not cur:
+            rec["dead_at"] = b
+            return rec
+    for j in range(1, e - b + 1):
+        cur = step(nfa, cur, data[b + j - 1])
+        pos = b + j
+        if index == 0:
+            if not cur:
+                rec["dead_at"] = pos
+                return rec
+            if accepts(nfa, cur):
+                rec["acc_after"][0] = pos
+                return rec
+            continue
+        if not cur:
+            rec["dead_at"] = pos
+            return rec
+        if accepts(nfa, cur):
+            for c in range(CHECKPOINTS):
+                if j > (1 << c) and rec["acc_after"][c] < 0:
+                    rec["acc_after"][c] = pos
+            if j > (1 << (CHECKPOINTS - 1)):
+                return rec
+        if j <= (1 << (CHECKPOINTS - 1)) and (j & (j - 1)) == 0:
+            rec["counts"][j.bit_length() - 1] = len(cur)
+    rec["end"] = set(cur)
+    return rec
+
+
+def run_fixup(nfa, data, chunks, recs):
+    r0 = recs[0]
+    if r0["acc_after"][0] >= 0:
+        return True, r0["acc_after"][0]
+    if r0["dead_at"] >= 0:
+        return False, 0
+    cur = r0["end"]
+    for (b, e), rk in zip(chunks[1:], recs[1:]):
+        matched = -1
+        j = 0
+        while b + j < e:
+            cur = step(nfa, cur, data[b + j])
+            j += 1
+            if not cur:
+                return False, 0
+            if accepts(nfa, cur):
+                return True, b + j
+            if j <= 32 and (j & (j - 1)) == 0 and len(cur) == rk["counts"][j.bit_length() - 1]:
+                matched = j.bit_length() - 1
+                break
+        if matched >= 0:
+            if rk["acc_after"][matched] >= 0:
+                return True, rk["acc_after"][matched]
+            if rk["dead_at"] >= 0:
+                return False, 0
+            if rk["end"] is not None:
+                cur = rk["end"]
+            else:
+                while b + j < e:
+                    cur = step(nfa, cur, data[b + j])
+                    j += 1
+    return False, 0
+
+
+def speculative(nfa, data: bytes, chunk: int):
+    n = len(data)
+    if n < 2 * chunk:
+        return simulate(nfa, data)
+    lists = first_lists(nfa)
+    count = n // chunk
+    bounds = [(k * chunk, (k + 1) * chunk if k < count - 1 else n) for k in range(count)]
+    recs = [run_chunk(nfa, data, b, e, k, lists) for k, (b, e) in enumerate(bounds)]
+    return run_fixup(nfa, data, bounds, recs)
+
+
+def _fuzz_nfa(rng, n, alpha, p_acc, p_any, max_eps):
+    b = NFABuilder()
+    for _ in range(n):
+        b.add_state(accept=rng.random() < p_acc)
+    b.set_start(rng.randrange(n))
+    for s in range(n):
+        for _ in range(rng.randint(0, 3)):
+            sym = ANY_SYMBOL if rng.random() < p_any else ord(rng.choice(alpha))
+            b.add_transition(s, sym, rng.randrange(n))
+        for _ in range(rng.randint(0, max_eps)):
+            b.add_epsilon(s, rng.randrange(n))
+    return b.build()
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_protocol_matches_the_oracle_on_fuzz(seed):
+    rng = random.Random(1000 + seed)
+    for _ in range(25):
+        nfa = _fuzz_nfa(rng, rng.randint(1, 40), "abc", 0.03, 0.05, rng.choice([0, 1, 2]))
+        for _ in range(4):
+            data = bytes(ord(rng.choice("abc")) for _ in range(rng.randint(0, 400)))
+            for chunk in (40, 64, 97):
+                assert speculative(nfa, data, chunk) == simulate(nfa, data)
+
+
+def test_protocol_on_live_walks_of_the_large_configuration():
+    b = W.c3("live", n_inputs=64)
+    nfa = b.automata[0]
+    idx = np.argsort(np.diff(b.offsets))[:12]
+    for i in idx:
+        data = b.inputs([int(i)])[0][:6000]
+        for chunk in (256, 1000):
+            assert speculative(nfa, data, chunk) == simulate(nfa, data)
