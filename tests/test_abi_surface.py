@@ -60,12 +60,27 @@ def test_python_binding_covers_the_header(lib):
     assert lib.gbfsm_abi_version() == native.ABI_VERSION
 
 
-def test_struct_layouts_match_the_header():
-    assert ctypes.sizeof(native.Edge) == 16
-    assert ctypes.sizeof(native.Plan) == 32
-    assert ctypes.sizeof(native.Task) == 16
-    assert ctypes.sizeof(native.NfaDev) == 16 + 5 * 8 + 16
-    assert ctypes.sizeof(native.DfaDev) == 16 + 8 + 8 + 8
+def test_struct_layouts_match_the_header(tmp_path):
+    """Compile a probe against include/gbfsm.h and compare every struct with ctypes."""
+    pairs = {"gbfsm_edge": native.Edge, "gbfsm_nfa_dev": native.NfaDev,
+             "gbfsm_dfa_dev": native.DfaDev, "gbfsm_plan": native.Plan,
+             "gbfsm_automaton": native.Automaton, "gbfsm_task": native.Task,
+             "gbfsm_chunk": native.Chunk}
+    src = tmp_path / "probe.c"
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gbfsm.h"', "int main(void) {"]
+    for name in pairs:
+        lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
+    lines.append('  printf("record %d\\n", GBFSM_CHUNK_RECORD_BYTES);')
+    lines.append("  return 0; }")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", str(REPO / "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    for name, cls in pairs.items():
+        assert int(out[name]) == ctypes.sizeof(cls), name
+    assert int(out["record"]) == native.CHUNK_RECORD_BYTES
+    assert np.dtype(native.CHUNK_DTYPE).itemsize == ctypes.sizeof(native.Chunk)
 
 
 def test_invalid_arguments_return_status_codes(lib):
