@@ -55,8 +55,8 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
-def _compile(src: Path, extra: list[str]) -> Path:
-    obj = OUT_DIR / (src.stem + ".o")
+def _compile(src: Path, extra: list[str], obj_dir: Path = OUT_DIR) -> Path:
+    obj = obj_dir / (src.stem + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -64,24 +64,32 @@ def _compile(src: Path, extra: list[str]) -> Path:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
-    """Compile every ``csrc/*.cu`` and link ``libgbfsm.so``; returns its path."""
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None,
+          out: Path | None = None) -> Path:
+    """Compile every ``csrc/*.cu`` and link ``libgbfsm.so``; returns its path.
+
+    ``extra`` adds nvcc flags (e.g. ``-DGBFSM_PERSIST_MIN_BLOCKS=4`` to build a tuning
+    variant); ``out`` writes the library somewhere else than the package directory (load
+    it with ``GBFSM_LIBRARY=<path>``).
+    """
+    lib = Path(out) if out else LIB
+    if not force and out is None and not extra and up_to_date():
         return LIB
-    OUT_DIR.mkdir(parents=True, exist_ok=True)
+    obj_dir = OUT_DIR if out is None else lib.parent / (lib.stem + "_objs")
+    obj_dir.mkdir(parents=True, exist_ok=True)
     extra = list(extra or [])
     srcs = sources()
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as pool:
-        objs = list(pool.map(lambda s: _compile(s, extra), srcs))
-    tmp = LIB.with_suffix(f".so.{os.getpid()}.tmp")
+        objs = list(pool.map(lambda s: _compile(s, extra, obj_dir), srcs))
+    tmp = lib.with_suffix(f".so.{os.getpid()}.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link of libgbfsm.so failed:\n{res.stderr}\n{res.stdout}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 def main(argv: list[str] | None = None) -> int:
@@ -89,7 +97,11 @@ def main(argv: list[str] | None = None) -> int:
     ap.add_argument("--force", action="store_true", help="rebuild even if up to date")
     ap.add_argument("--ptxas-info", action="store_true",
                     help="print registers / spills / shared memory per kernel (-Xptxas -v)")
+    ap.add_argument("--define", "-D", action="append", default=[],
+                    help="preprocessor define for a tuning variant, e.g. GBFSM_PERSIST_MIN_BLOCKS=4")
+    ap.add_argument("--out", default=None, help="write the library to this path instead")
     args = ap.parse_args(argv)
+    defines = [f"-D{d}" for d in args.define]
     extra = ["-Xptxas", "-v"] if args.ptxas_info else []
     if args.ptxas_info:
         OUT_DIR.mkdir(parents=True, exist_ok=True)
@@ -100,7 +112,8 @@ def main(argv: list[str] | None = None) -> int:
             sys.stdout.write(res.stderr)
             if res.returncode:
                 return res.returncode
-    build(force=args.force, verbose=True)
+    build(force=args.force, verbose=True, extra=defines or None,
+          out=Path(args.out) if args.out else None)
     return 0
 
 

@@ -66,6 +66,63 @@ __device__ __forceinline__ uint32_t byte_of(const uint4 &v, int k) {
     return (w >> ((k & 3) * 8)) & 0xffu;
 }
 
+// Sequential reader of one input's bytes: 16-byte loads (L1::no_allocate), the next
+// block fetched one block ahead of use; bytes are shifted out of four 32-bit words with
+// funnel shifts. Reads never leave the 16-byte blocks that contain input bytes.
+struct ByteStream {
+    const uint8_t *blk;
+    const uint8_t *end;
+    uint4 ahead;
+    uint32_t w0, w1, w2, w3;
+    int left;
+
+    __device__ __forceinline__ void shift_bytes(int r) {
+        w0 = __funnelshift_r(w0, w1, r);
+        w1 = __funnelshift_r(w1, w2, r);
+        w2 = __funnelshift_r(w2, w3, r);
+        w3 >>= r;
+    }
+
+    __device__ __forceinline__ void init(const uint8_t *in, int64_t len) {
+        end = in + len;
+        const uint64_t a = reinterpret_cast<uint64_t>(in);
+        blk = reinterpret_cast<const uint8_t *>(a & ~15ull);
+        const int skip = (int)(a & 15ull);
+        uint4 c = make_uint4(0, 0, 0, 0);
+        ahead = make_uint4(0, 0, 0, 0);
+        if (len > 0) c = ld_stream16(blk);
+        if (blk + 16 < end) ahead = ld_stream16(blk + 16);
+        w0 = c.x;
+        w1 = c.y;
+        w2 = c.z;
+        w3 = c.w;
+        for (int q = 0; q < (skip >> 2); ++q) {
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = 0;
+        }
+        if (skip & 3) shift_bytes((skip & 3) * 8);
+        left = 16 - skip;
+    }
+
+    __device__ __forceinline__ uint32_t next() {
+        if (left == 0) {
+            blk += 16;
+            w0 = ahead.x;
+            w1 = ahead.y;
+            w2 = ahead.z;
+            w3 = ahead.w;
+            if (blk + 16 < end) ahead = ld_stream16(blk + 16);
+            left = 16;
+        }
+        const uint32_t b = w0 & 0xffu;
+        shift_bytes(8);
+        --left;
+        return b;
+    }
+};
+
 // Inclusive warp prefix sum of `x` (all 32 lanes participate).
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x) {
     const uint32_t lane = lane_id();

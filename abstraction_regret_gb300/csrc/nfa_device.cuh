@@ -25,6 +25,14 @@
 
 #include "common.cuh"
 
+// Paths taken rarely per byte (set-size changes, epsilon closure, mode switches). They
+// are inlined by default: kept out of line (-DGBFSM_COLD=__noinline__) the per-byte loop
+// needs fewer registers, but the stepper's state then lives in local memory, which
+// measured slower on GB300 (c3-sustained: 2.9 vs 3.5 GB/s) than two CTAs per SM.
+#ifndef GBFSM_COLD
+#define GBFSM_COLD __forceinline__
+#endif
+
 namespace gbfsm {
 
 constexpr int kFlagTimeout = -1;  // flags[] value written when a bounded wait gave up
@@ -35,8 +43,8 @@ struct WarpScratch {
     uint64_t *D;   // [W] dense current set; all-zero while sparse
     uint64_t *FA;  // [W] dense closure frontier; all-zero between steps
     uint64_t *FB;  // [W] dense closure frontier (next round); all-zero between steps
-    uint4 *LA;     // [C] current member list
-    uint4 *LB;     // [C] next member list
+    uint4 *LA;     // [max(C, 32)] current member list
+    uint4 *LB;     // [max(C, 32)] next member list (also the REG-mode compaction buffer)
     int C;         // list capacity; 0 = dense only
 };
 
@@ -299,7 +307,7 @@ struct WarpNfa {
     }
 
     // The set just built in V (n members; LB holds them when !dense_now) becomes current.
-    __device__ int finish_general(int n, bool dense_now, uint32_t info_or) {
+    __device__ GBFSM_COLD int finish_general(int n, bool dense_now, uint32_t info_or) {
         const uint32_t lane = lane_id();
         __syncwarp();
         const uint32_t flags = __reduce_or_sync(GBFSM_FULL_MASK, info_or);
@@ -340,7 +348,7 @@ struct WarpNfa {
     }
 
     // Start configuration: closure({start}).
-    __device__ int init_start() {
+    __device__ GBFSM_COLD int init_start() {
         const uint4 rec = state_record((uint32_t)A.start_state);
         if (S.C > 0 && !(rec.y & GBFSM_EDGE_HAS_EPS)) {
             mode = kReg;
@@ -366,7 +374,7 @@ struct WarpNfa {
         return finish_general(n, dense_now, info_or);
     }
 
-    __device__ int step_general(uint32_t sym) {
+    __device__ GBFSM_COLD int step_general(uint32_t sym) {
         const uint32_t lane = lane_id();
         if (mode == kReg) {
             if (m <= S.C) {
@@ -411,29 +419,39 @@ struct WarpNfa {
         return finish_general(n, dense_now, info_or);
     }
 
-    // REG-mode step: at most 32 members with at most 32 edges in total.
+    // REG-mode step: at most 32 members with at most 32 edges in total. The common case
+    // (at most 4 members of at most 8 edges) gives each member 8 fixed lanes, so no scan
+    // is needed to spread the edges; otherwise a warp scan flattens them.
     __device__ int step_reg(uint32_t sym) {
         const uint32_t lane = lane_id();
         const uint32_t deg = ((int)lane < m) ? mine.w - mine.z : 0u;
-        const uint32_t incl = warp_inclusive_scan(deg);
-        const uint32_t total = __shfl_sync(GBFSM_FULL_MASK, incl, 31);
-        if (total > 32u) return step_general(sym);
-        const uint32_t excl = incl - deg;
-        uint32_t owner = 0;
-        if (m > 1) {
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        bool have;
+        if (m <= 4 && __ballot_sync(GBFSM_FULL_MASK, deg > 8u) == 0u) {
+            const uint32_t mem = lane >> 3;
+            const uint32_t rb = __shfl_sync(GBFSM_FULL_MASK, mine.z, mem);
+            const uint32_t dg = __shfl_sync(GBFSM_FULL_MASK, deg, mem);
+            have = (lane & 7u) < dg;  // dg is 0 for lanes past the last member
+            if (have) rec = load_edge<kStaged>(R.sym_edges + rb + (lane & 7u));
+        } else {
+            const uint32_t incl = warp_inclusive_scan(deg);
+            const uint32_t total = __shfl_sync(GBFSM_FULL_MASK, incl, 31);
+            if (total > 32u) return step_general(sym);
+            const uint32_t excl = incl - deg;
+            uint32_t owner = 0;
 #pragma unroll
             for (uint32_t step = 16; step >= 1; step >>= 1) {
                 const uint32_t cand = owner + step;
                 const uint32_t e = __shfl_sync(GBFSM_FULL_MASK, excl, cand);
                 if (e <= lane) owner = cand;
             }
+            const uint32_t orb = __shfl_sync(GBFSM_FULL_MASK, mine.z, owner);
+            const uint32_t oex = __shfl_sync(GBFSM_FULL_MASK, excl, owner);
+            have = lane < total;
+            if (have) rec = load_edge<kStaged>(R.sym_edges + orb + (lane - oex));
         }
-        const uint32_t orb = __shfl_sync(GBFSM_FULL_MASK, mine.z, owner);
-        const uint32_t oex = __shfl_sync(GBFSM_FULL_MASK, excl, owner);
         bool match = false;
-        uint4 rec = make_uint4(0, 0, 0, 0);
-        if (lane < total) {
-            rec = load_edge<kStaged>(R.sym_edges + orb + (lane - oex));
+        if (have) {
             const uint32_t es = rec.y & GBFSM_EDGE_SYMBOL_MASK;
             match = (es == sym) || (es == GBFSM_ANY_SYMBOL);
         }
@@ -446,8 +464,8 @@ struct WarpNfa {
             m = 0;
             return kDead;
         }
-        const uint32_t acc = __ballot_sync(GBFSM_FULL_MASK, fresh && (rec.y & GBFSM_EDGE_ACCEPT));
-        if (has_eps && __ballot_sync(GBFSM_FULL_MASK, fresh && (rec.y & GBFSM_EDGE_HAS_EPS))) {
+        const uint32_t info = __reduce_or_sync(GBFSM_FULL_MASK, fresh ? rec.y : 0u);
+        if (has_eps && (info & GBFSM_EDGE_HAS_EPS)) {
             // epsilon closure needed: continue through the shared-memory path
             if (fresh) {
                 const int pos = __popc(F & lanemask_lt());
@@ -467,11 +485,13 @@ struct WarpNfa {
             }
             return finish_general(nn, dense_now, info_or);
         }
-        const uint32_t src = select_bit(F, min(lane, (uint32_t)(n - 1)));
-        mine = shfl_rec(rec, src);
-        if ((int)lane >= n) mine = make_uint4(0, 0, 0, 0);
+        // compact the new members into lanes 0..n-1 through the (32-slot) list buffer
+        if (fresh) S.LB[__popc(F & lanemask_lt())] = rec;
+        __syncwarp();
+        mine = ((int)lane < n) ? S.LB[lane] : make_uint4(0, 0, 0, 0);
+        __syncwarp();
         m = n;
-        return acc ? kAccept : kAlive;
+        return (info & GBFSM_EDGE_ACCEPT) ? kAccept : kAlive;
     }
 
     __device__ __forceinline__ int step(uint32_t sym) {
@@ -480,7 +500,7 @@ struct WarpNfa {
 
     // Start from the set of records recs[rb .. re) (distinct states), closed under epsilon
     // edges: the speculative superset of a chunk (first_edges of one byte).
-    __device__ int init_records(const gbfsm_edge *recs, uint32_t rb, uint32_t re) {
+    __device__ GBFSM_COLD int init_records(const gbfsm_edge *recs, uint32_t rb, uint32_t re) {
         const uint32_t lane = lane_id();
         const uint32_t cnt = re - rb;
         if (cnt == 0) {
@@ -514,7 +534,7 @@ struct WarpNfa {
     }
 
     // Start from the states ids[0 .. count) (distinct, already closed under epsilon).
-    __device__ void init_ids(const uint32_t *ids, int count) {
+    __device__ GBFSM_COLD void init_ids(const uint32_t *ids, int count) {
         const uint32_t lane = lane_id();
         if (count <= 32) {
             mine = ((int)lane < count) ? state_record(ids[lane]) : make_uint4(0, 0, 0, 0);
@@ -572,25 +592,12 @@ __device__ Verdict simulate_warp(const gbfsm_nfa_dev &A, const Rows &R, const ui
         w.cleanup();
         return v;
     }
-    // input bytes: 16-byte blocks, the next block loaded one block ahead of use
-    const uint8_t *end = in + len;
-    const uint64_t addr = reinterpret_cast<uint64_t>(in);
-    const uint8_t *blk = reinterpret_cast<const uint8_t *>(addr & ~15ull);
-    int k = (int)(addr & 15ull);
-    uint4 chunk = make_uint4(0, 0, 0, 0), ahead = make_uint4(0, 0, 0, 0);
-    if (len > 0) chunk = ld_stream16(blk);
-    if (blk + 16 < end) ahead = ld_stream16(blk + 16);
+    ByteStream bytes;
+    bytes.init(in, len);
     int64_t pos = 0;
     v.examined = len;
     while (pos < len) {
-        if (k == 16) {
-            blk += 16;
-            k = 0;
-            chunk = ahead;
-            if (blk + 16 < end) ahead = ld_stream16(blk + 16);
-        }
-        const uint32_t sym = byte_of(chunk, k);
-        ++k;
+        const uint32_t sym = bytes.next();
         ++pos;
         ev = w.step(sym);
         if (ev == kDead) {

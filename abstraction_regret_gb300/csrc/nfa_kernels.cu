@@ -13,6 +13,8 @@
 //
 // With plan.stage the edge rows are copied into shared memory by the TMA engine
 // (cp.async.bulk) once per CTA when they fit next to the per-warp scratch.
+#include <algorithm>
+
 #include "common.cuh"
 #include "engine.hpp"
 #include "nfa_device.cuh"
@@ -78,12 +80,12 @@ __global__ void __launch_bounds__(kMaxBlockThreads) nfa_warp_kernel(gbfsm_nfa_de
     WarpScratch S;
     S.C = wp.C;
     // V and the lists first, then D/FA/FB, each in shared memory or the global slice
-    const size_t vpart = wbytes + (size_t)32u * (uint32_t)wp.C;
+    const size_t vpart = wbytes + (size_t)32u * (uint32_t)max(wp.C, 32);
     uint8_t *vp = wp.v_in_smem ? sp : gp;
     uint8_t *dp = wp.dense_in_smem ? sp + vpart : (wp.v_in_smem ? gp : gp + vpart);
     S.V = reinterpret_cast<uint64_t *>(vp);
     S.LA = reinterpret_cast<uint4 *>(vp + wbytes);
-    S.LB = S.LA + wp.C;
+    S.LB = S.LA + max(wp.C, 32);
     S.D = reinterpret_cast<uint64_t *>(dp);
     S.FA = reinterpret_cast<uint64_t *>(dp + wbytes);
     S.FB = reinterpret_cast<uint64_t *>(dp + 2 * wbytes);
@@ -337,7 +339,7 @@ gbfsm_status make_warp_plan(const gbfsm_nfa_dev &a, int32_t n_inputs, const gbfs
     wp.warps_per_cta = threads / 32;
     const size_t budget = (size_t)smem_optin() - kSmemReserve;
     const uint32_t wbytes = pad16((uint64_t)wp.W * 8u);
-    const size_t vpart = wbytes + (size_t)32u * (uint32_t)wp.C;
+    const size_t vpart = wbytes + (size_t)32u * (uint32_t)std::max(wp.C, 32);
     const size_t dpart = 3u * (size_t)wbytes;
     uint32_t stage = 0;
     if (p.stage) {

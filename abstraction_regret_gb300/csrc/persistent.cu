@@ -25,6 +25,12 @@ namespace gbfsm {
 namespace {
 
 constexpr int kPersistThreads = 256;  // 8 warps per CTA by default
+// CTAs of kPersistThreads per SM the register allocation must allow (the per-byte loop is
+// latency-bound: more resident warps means more chains in flight).
+#ifndef GBFSM_PERSIST_MIN_BLOCKS
+#define GBFSM_PERSIST_MIN_BLOCKS 2
+#endif
+constexpr int kPersistMinBlocks = GBFSM_PERSIST_MIN_BLOCKS;
 
 struct PersistLayout {
     int Wmax;
@@ -42,7 +48,7 @@ PersistLayout persist_layout(int32_t max_words, const gbfsm_plan &p) {
     const int threads = p.block_threads > 0 ? p.block_threads : kPersistThreads;
     L.wpc = threads / 32;
     L.wbytes = pad16((uint64_t)L.Wmax * 8u);
-    L.smem_per_warp = L.wbytes + 32u * (uint32_t)L.C;
+    L.smem_per_warp = L.wbytes + 32u * (uint32_t)max(L.C, 32);
     L.global_per_warp = 3u * (size_t)L.wbytes;
     return L;
 }
@@ -99,26 +105,12 @@ __device__ void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S
             stopped = true;
         }
     }
-    // stream the chunk's bytes 16 at a time, one block ahead
-    const uint8_t *in = base + b;
     const int64_t len = e - b;
-    const uint8_t *end = in + len;
-    const uint64_t addr = reinterpret_cast<uint64_t>(in);
-    const uint8_t *blk = reinterpret_cast<const uint8_t *>(addr & ~15ull);
-    int k = (int)(addr & 15ull);
-    uint4 chunk = make_uint4(0, 0, 0, 0), ahead = make_uint4(0, 0, 0, 0);
-    if (!stopped && len > 0) chunk = ld_stream16(blk);
-    if (!stopped && blk + 16 < end) ahead = ld_stream16(blk + 16);
+    ByteStream bytes;
+    bytes.init(base + b, stopped ? 0 : len);
     int64_t j = 0;
     while (!stopped && j < len) {
-        if (k == 16) {
-            blk += 16;
-            k = 0;
-            chunk = ahead;
-            if (blk + 16 < end) ahead = ld_stream16(blk + 16);
-        }
-        ev = w.step(byte_of(chunk, k));
-        ++k;
+        ev = w.step(bytes.next());
         ++j;
         const int32_t pos = (int32_t)(b + j);
         if (index == 0) {
@@ -237,7 +229,7 @@ __device__ Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratc
     return v;
 }
 
-__global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
+__global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persistent_kernel(
     const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
     int32_t n_tasks, const int32_t *__restrict__ input_ids, const uint8_t *__restrict__ data,
     const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends,
@@ -252,7 +244,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads) persistent_kernel(
     WarpScratch S;
     S.V = reinterpret_cast<uint64_t *>(sp);
     S.LA = reinterpret_cast<uint4 *>(sp + L.wbytes);
-    S.LB = S.LA + L.C;
+    S.LB = S.LA + max(L.C, 32);
     S.D = reinterpret_cast<uint64_t *>(gp);
     S.FA = reinterpret_cast<uint64_t *>(gp + L.wbytes);
     S.FB = reinterpret_cast<uint64_t *>(gp + 2 * L.wbytes);

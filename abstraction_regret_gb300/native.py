@@ -14,9 +14,12 @@ native/include/common.cuh:63-71).
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libgbfsm.so"
+# The in-tree build; GBFSM_LIBRARY points at another build of the same ABI (e.g. a
+# tuning variant made with ``python -m abstraction_regret_gb300.build --out``).
+LIB_PATH = Path(os.environ.get("GBFSM_LIBRARY") or Path(__file__).resolve().parent / "libgbfsm.so")
 
 OK, INVALID_ARG, UNSUPPORTED, CUDA_ERROR, TIMEOUT, OOM = range(6)
 
