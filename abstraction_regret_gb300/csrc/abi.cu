@@ -237,16 +237,16 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
                                   int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
                                   const int32_t *input_ids, const uint8_t *data,
                                   const int64_t *offsets, const int64_t *ends,
-                                  const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
-                                  int32_t *lens, int32_t *examined, void *workspace,
-                                  size_t workspace_bytes, const gbfsm_plan *plan, void *stream) {
+                                  const gbfsm_chunk_io *chunk_io, int32_t *flags, int32_t *lens,
+                                  int32_t *examined, void *workspace, size_t workspace_bytes,
+                                  const gbfsm_plan *plan, void *stream) {
     if (n_tasks < 0 || n_automata < 0) return fail(GBFSM_INVALID_ARG, "negative task count");
     if (n_tasks > 0 && (!table || !tasks || !input_ids || !data || !offsets || !flags || !lens))
         return fail(GBFSM_INVALID_ARG, "NULL array passed to gbfsm_persistent_run");
     if (max_words < 1) return fail(GBFSM_INVALID_ARG, "max_words must be >= 1");
     const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
     return launch_persistent(table, max_words, tasks, n_tasks, input_ids, data, offsets, ends,
-                             chunks, chunk_records, flags, lens, examined, workspace,
+                             chunk_io, flags, lens, examined, workspace,
                              workspace_bytes, p,
                              static_cast<cudaStream_t>(stream));
 }

@@ -68,7 +68,7 @@ gbfsm_status launch_dfa_walk(const gbfsm_dfa_dev &d, const gbfsm_plan &p, const 
 gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
                                const uint8_t *data, const int64_t *offsets, const int64_t *ends,
-                               const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
+                               const gbfsm_chunk_io *chunk_io, int32_t *flags,
                                int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream);
 size_t persistent_workspace_bytes(int32_t max_words, const gbfsm_plan &p);

@@ -229,12 +229,166 @@ __device__ Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratc
     return v;
 }
 
+// LANES task body: one chunk per lane, the set held in registers (at most kLaneCap
+// members: id and edge-row range each). Same protocol and record as run_chunk; a chunk
+// whose set outgrows the lane returns false without writing its record. The first step
+// of a speculative chunk starts from the two-byte superset pair_edges of the bytes
+// before it; each step scans a member's edge labels (edge_sym, uint16) and loads the
+// 16-byte record only of an edge that matches.
+constexpr int kLaneCap = 8;
+
+__device__ bool run_chunk_lane(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b, int64_t e,
+                               int index, ChunkRecord *rec) {
+    uint32_t ct[kLaneCap], crb[kLaneCap], cre[kLaneCap];
+    int m = 0;
+    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        counts[c] = 0;
+        acc_after[c] = -1;
+    }
+#pragma unroll
+    for (int i = 0; i < kLaneCap; ++i) ct[i] = crb[i] = cre[i] = 0;
+    int32_t dead_at = -1;
+    bool stopped = false;
+    if (index == 0) {
+        const uint32_t s = (uint32_t)A.start_state;
+        ct[0] = s;
+        crb[0] = __ldg(A.sym_row + s);
+        cre[0] = __ldg(A.sym_row + s + 1);
+        m = 1;
+        if ((__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
+             (s & 63u)) & 1ull) {
+            acc_after[0] = 0;
+            stopped = true;
+        }
+    } else {
+        const uint32_t key = (uint32_t)__ldg(base + b - 2) * 256u + (uint32_t)__ldg(base + b - 1);
+        const uint32_t pr = __ldg(A.pair_row + key), pe = __ldg(A.pair_row + key + 1);
+        if (pe - pr > (uint32_t)kLaneCap) return false;
+        m = (int)(pe - pr);
+#pragma unroll
+        for (int i = 0; i < kLaneCap; ++i) {
+            if (i < m) {
+                const uint4 r = ld_edge(A.pair_edges + pr + i);
+                ct[i] = r.x;
+                crb[i] = r.z;
+                cre[i] = r.w;
+            }
+        }
+        if (m == 0) {
+            dead_at = (int32_t)b;
+            stopped = true;
+        }
+    }
+    const int64_t len = e - b;
+    ByteStream bytes;
+    bytes.init(base + b, stopped ? 0 : len);
+    int64_t j = 0;
+    while (!stopped && j < len) {
+        const uint32_t sym = bytes.next();
+        ++j;
+        uint32_t nt[kLaneCap], nrb[kLaneCap], nre[kLaneCap];
+        int n = 0;
+        bool acc = false, ovf = false;
+#pragma unroll
+        for (int i = 0; i < kLaneCap; ++i) {
+            if (i < m) {
+                for (uint32_t k = crb[i]; k < cre[i]; ++k) {
+                    const uint32_t es = __ldg(A.edge_sym + k);
+                    if (es != sym && es != (uint32_t)GBFSM_ANY_SYMBOL) continue;
+                    const uint4 r = ld_edge(A.sym_edges + k);
+                    bool dup = false;
+#pragma unroll
+                    for (int q = 0; q < kLaneCap; ++q) dup |= (q < n) && (nt[q] == r.x);
+                    if (dup) continue;
+                    if (n == kLaneCap) {
+                        ovf = true;
+                        continue;
+                    }
+#pragma unroll
+                    for (int q = 0; q < kLaneCap; ++q) {
+                        if (q == n) {
+                            nt[q] = r.x;
+                            nrb[q] = r.z;
+                            nre[q] = r.w;
+                        }
+                    }
+                    ++n;
+                    acc |= (r.y & GBFSM_EDGE_ACCEPT) != 0;
+                }
+            }
+        }
+        if (ovf) return false;
+#pragma unroll
+        for (int q = 0; q < kLaneCap; ++q) {
+            ct[q] = nt[q];
+            crb[q] = nrb[q];
+            cre[q] = nre[q];
+        }
+        m = n;
+        const int32_t pos = (int32_t)(b + j);
+        if (index == 0) {
+            if (m == 0) {
+                dead_at = pos;
+                stopped = true;
+            } else if (acc) {
+                acc_after[0] = pos;
+                stopped = true;
+            }
+            continue;
+        }
+        if (m == 0) {
+            dead_at = pos;
+            stopped = true;
+            break;
+        }
+        if (acc) {
+#pragma unroll
+            for (int c = 0; c < kCheckpoints; ++c)
+                if (j > (1 << c) && acc_after[c] < 0) acc_after[c] = pos;
+            if (j > (1 << (kCheckpoints - 1))) stopped = true;
+        }
+        if (j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) {
+            const int c = 31 - __clz((int)j);
+#pragma unroll
+            for (int q = 0; q < kCheckpoints; ++q)
+                if (q == c) counts[q] = m;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        rec->counts[c] = counts[c];
+        rec->acc_after[c] = acc_after[c];
+    }
+    rec->dead_at = dead_at;
+    rec->end_count = stopped ? -1 : m;
+    if (!stopped) {
+#pragma unroll
+        for (int q = 0; q < kLaneCap; ++q)
+            if (q < m) rec->end_ids[q] = ct[q];
+    }
+    return true;
+}
+
+// Device pointers of the chunk machinery, passed by value to the kernel.
+struct ChunkIO {
+    const gbfsm_chunk *chunks;
+    ChunkRecord *records;
+    gbfsm_task *overflow_tasks;
+    int32_t *overflow_count;
+    const int32_t *task_count;
+};
+
 __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persistent_kernel(
     const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
     int32_t n_tasks, const int32_t *__restrict__ input_ids, const uint8_t *__restrict__ data,
-    const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends,
-    const gbfsm_chunk *__restrict__ chunks, ChunkRecord *records, int32_t *flags, int32_t *lens,
-    int32_t *examined, PersistLayout L, uint32_t *ticket, uint8_t *gws) {
+    const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends, ChunkIO io,
+    int32_t *flags, int32_t *lens, int32_t *examined, PersistLayout L, uint32_t *ticket,
+    uint8_t *gws) {
+    const gbfsm_chunk *__restrict__ chunks = io.chunks;
+    ChunkRecord *records = io.records;
+    if (io.task_count) n_tasks = min(n_tasks, *io.task_count);
     extern __shared__ __align__(16) uint8_t smem[];
     const int warp = (int)(threadIdx.x >> 5);
     const uint32_t lane = lane_id();
@@ -269,6 +423,25 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
             R.eps_row = nfa.eps_row;
             R.eps_edges = nfa.eps_edges;
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
+            if (task.kind == GBFSM_TASK_LANES) {
+                if ((int)lane < task.count) {
+                    const int cid = task.first + (int)lane;
+                    const gbfsm_chunk ch = chunks[cid];
+                    const int64_t off = offsets[ch.input];
+                    if (!run_chunk_lane(nfa, data + off, ch.begin - off, ch.end - off, ch.index,
+                                        records + cid)) {
+                        const int slot = atomicAdd(io.overflow_count, 1);
+                        gbfsm_task spill;
+                        spill.automaton = task.automaton;
+                        spill.first = cid;
+                        spill.count = 1;
+                        spill.kind = GBFSM_TASK_CHUNK;
+                        io.overflow_tasks[slot] = spill;
+                    }
+                }
+                __syncwarp();
+                continue;
+            }
             if (task.kind == GBFSM_TASK_CHUNK) {
                 const gbfsm_chunk ch = chunks[task.first];
                 const int64_t off = offsets[ch.input];
@@ -382,7 +555,7 @@ int32_t persistent_ctas_query(const PersistLayout &L, const gbfsm_plan &p) {
 gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
                                const uint8_t *data, const int64_t *offsets, const int64_t *ends,
-                               const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
+                               const gbfsm_chunk_io *chunk_io, int32_t *flags,
                                int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream) {
     const PersistLayout L = persist_layout(max_words, p);
@@ -398,6 +571,14 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
         return fail(GBFSM_INVALID_ARG, "persistent workspace too small: %zu < %zu bytes",
                     workspace_bytes, need);
     if (n_tasks <= 0) return GBFSM_OK;
+    ChunkIO io{nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (chunk_io) {
+        io.chunks = chunk_io->chunks;
+        io.records = static_cast<ChunkRecord *>(chunk_io->records);
+        io.overflow_tasks = chunk_io->overflow_tasks;
+        io.overflow_count = chunk_io->overflow_count;
+        io.task_count = chunk_io->task_count;
+    }
     uint32_t *ticket = static_cast<uint32_t *>(workspace);
     uint8_t *gws = static_cast<uint8_t *>(workspace) + 256;
     GBFSM_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream));
@@ -406,9 +587,8 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
     const int needed = (n_tasks + L.wpc - 1) / L.wpc;
     if (grid > needed) grid = needed;
     persistent_kernel<<<grid, L.wpc * 32, smem, stream>>>(table, tasks, n_tasks, input_ids, data,
-                                                          offsets, ends, chunks,
-                                                          static_cast<ChunkRecord *>(chunk_records),
-                                                          flags, lens, examined, L, ticket, gws);
+                                                          offsets, ends, io, flags, lens,
+                                                          examined, L, ticket, gws);
     GBFSM_LAUNCH_CHECK("persistent_kernel launch");
     return GBFSM_OK;
 }

@@ -78,10 +78,59 @@ def first_lists(nfa, limit: int = SUPERSET_LIMIT):
     row = np.zeros(257, dtype=np.int64)
     np.cumsum(np.bincount(c, minlength=256), out=row[1:])
     srp = np.asarray(nfa.sym_row_ptr, dtype=np.int64)
-    erp = np.asarray(nfa.eps_row_ptr, dtype=np.int64)
+    recs = np.stack([t, _info(nfa, t), srp[t], srp[t + 1]], axis=1).astype(np.uint32)
+    return row.astype(np.int32), recs
+
+
+PAIR_LIMIT = 1 << 24  # records; above this an automaton gets no two-byte superset table
+
+
+def _info(nfa, t: np.ndarray) -> np.ndarray:
     acc = np.asarray(nfa.accept, dtype=bool)
-    info = (acc[t].astype(np.int64) << 9) | ((erp[t + 1] > erp[t]).astype(np.int64) << 10)
-    recs = np.stack([t, info, srp[t], srp[t + 1]], axis=1).astype(np.uint32)
+    erp = np.asarray(nfa.eps_row_ptr, dtype=np.int64)
+    return (acc[t].astype(np.int64) << 9) | ((erp[t + 1] > erp[t]).astype(np.int64) << 10)
+
+
+def pair_lists(nfa, first, limit: int = PAIR_LIMIT):
+    """Two-byte supersets for an automaton without epsilon edges.
+
+    For bytes c1, c2: the distinct targets, reachable by a c2 (or ANY) edge, of the states
+    in ``first`` for c1 -- i.e. every state the automaton can occupy after reading c1 c2,
+    from any set. Returns ``(row int32[65537], records uint32[k, 4])`` or ``None`` (epsilon
+    edges, no first lists, or more than ``limit`` records).
+    """
+    if first is None or int(np.asarray(nfa.eps_targets).size):
+        return None
+    row1, recs1 = first
+    n = int(nfa.num_states)
+    srp = np.asarray(nfa.sym_row_ptr, dtype=np.int64)
+    syms = np.asarray(nfa.sym_symbols, dtype=np.int64)
+    tgts = np.asarray(nfa.sym_targets, dtype=np.int64)
+    states = recs1[:, 0].astype(np.int64)
+    c1_of = np.repeat(np.arange(256, dtype=np.int64), np.diff(row1.astype(np.int64)))
+    deg = srp[states + 1] - srp[states]
+    total = int(deg.sum())
+    if total > 4 * limit:
+        return None
+    offs = np.cumsum(deg) - deg
+    edge = np.arange(total, dtype=np.int64) - np.repeat(offs, deg) + np.repeat(srp[states], deg)
+    c1_e = np.repeat(c1_of, deg)
+    e_sym, e_tgt = syms[edge], tgts[edge]
+    plain = e_sym != ANY_SYMBOL
+    keys = (c1_e[plain] * 256 + e_sym[plain]) * n + e_tgt[plain]
+    if (~plain).any():
+        c1_a, t_a = c1_e[~plain], e_tgt[~plain]
+        if c1_a.size * 256 > 4 * limit:
+            return None
+        keys = np.concatenate([keys, ((c1_a[:, None] * 256 + np.arange(256)[None, :]) * n
+                                      + t_a[:, None]).ravel()])
+    keys = np.unique(keys)
+    if keys.size > limit:
+        return None
+    pair, t = keys // n, keys % n
+    row = np.zeros(65537, dtype=np.int64)
+    np.cumsum(np.bincount(pair, minlength=65536), out=row[1:])
+    recs = np.stack([t, _info(nfa, t), srp[t], srp[t + 1]], axis=1).astype(np.uint32)
     return row.astype(np.int32), recs
 
 
@@ -158,6 +207,24 @@ class DeviceNFA:
                         torch.from_numpy(np.ascontiguousarray(recs).view(np.uint8).ravel()))
             d.first_row = self.first_row.data_ptr()
             d.first_edges = self.first_edges.data_ptr()
+        pairs = pair_lists(nfa, lists)
+        self.lanes = pairs is not None
+        self.pair_mean = float(np.diff(pairs[0]).mean()) if pairs is not None else float("inf")
+        if pairs is not None:
+            prow, precs = pairs
+            with torch.cuda.device(dev):
+                self.edge_sym = _padded(max(1, nnz), 2, dev, torch.int16)
+                if nnz:
+                    self.edge_sym[:nnz].copy_(torch.from_numpy(
+                        np.ascontiguousarray(ssy, dtype=np.int16)))
+                self.pair_row = torch.from_numpy(np.ascontiguousarray(prow)).to(dev)
+                self.pair_edges = _padded(max(1, precs.shape[0]), 16, dev)
+                if precs.size:
+                    self.pair_edges[: precs.nbytes].copy_(
+                        torch.from_numpy(np.ascontiguousarray(precs).view(np.uint8).ravel()))
+            d.edge_sym = self.edge_sym.data_ptr()
+            d.pair_row = self.pair_row.data_ptr()
+            d.pair_edges = self.pair_edges.data_ptr()
         self.desc = d
 
     @property

@@ -45,6 +45,10 @@ from .staging import Results, Staging
 DFA_GROUP = 32
 NFA_BYTE_WEIGHT = 4  # task-ordering weight of an NFA byte relative to a DFA byte
 MIN_CHUNK = 256      # shortest speculative chunk (bytes)
+LANE_GROUP = 32      # chunks per LANES task (one per lane)
+# an automaton's chunks run one per lane when its two-byte supersets are this small on
+# average (the lane holds at most native.LANE_CAPACITY states; larger sets spill to warps)
+LANE_PAIR_MEAN = 4.0
 
 
 @dataclass
@@ -54,6 +58,7 @@ class NfaChoice:
     technique: int = native.TECH_COMPACT  # TECH_COMPACT or TECH_WARP
     list_capacity: int = 128
     speculate: bool = True                # allow chunked speculation for long inputs
+    lanes: bool = True                    # allow one-lane-per-chunk speculation
 
 
 @dataclass
@@ -63,8 +68,10 @@ class TaskPlan:
     tasks_a: np.ndarray    # int32 [na, 4]: WHOLE and CHUNK tasks (first launch)
     tasks_b: np.ndarray    # int32 [nb, 4]: FIXUP tasks (second launch)
     input_ids: np.ndarray  # int32 [n]
-    chunks: np.ndarray     # CHUNK_DTYPE [nc]
-    chunk_bytes: int
+    chunks: np.ndarray     # CHUNK_DTYPE [nc] (lane chunks first)
+    chunk_bytes: int       # chunk size of warp-simulated chunks (0: none)
+    lane_chunks: int = 0   # chunks run one per lane (the first lane_chunks of `chunks`)
+    lane_chunk_bytes: int = 0
 
 
 class DeviceTasks:
@@ -74,6 +81,18 @@ class DeviceTasks:
         self.device = device
         self.cap_t = self.cap_i = self.cap_c = 0
         self.na = self.nb = self.nc = 0
+        self.n_lane_chunks = 0
+
+    def chunk_io(self, overflow_count: bool = False) -> native.ChunkIO:
+        io = native.ChunkIO()
+        if self.nc:
+            io.chunks = self.d_chunks.data_ptr()
+            io.records = self.d_records.data_ptr()
+            io.overflow_tasks = self.d_overflow.data_ptr()
+            io.overflow_count = self.d_overflow_count.data_ptr()
+            if overflow_count:
+                io.task_count = self.d_overflow_count.data_ptr()
+        return io
 
     def _ensure(self, n_tasks: int, n_ids: int, n_chunks: int) -> None:
         dev = self.device
@@ -91,6 +110,8 @@ class DeviceTasks:
             self.d_chunks = torch.empty(self.cap_c * 24, dtype=torch.uint8, device=dev)
             self.d_records = torch.empty(self.cap_c * native.CHUNK_RECORD_BYTES,
                                          dtype=torch.uint8, device=dev)
+            self.d_overflow = torch.empty(self.cap_c * 4, dtype=torch.int32, device=dev)
+            self.d_overflow_count = torch.zeros(4, dtype=torch.int32, device=dev)
 
     def upload(self, plan: TaskPlan, stream) -> None:
         """Copy a plan into the pinned buffers and enqueue its host->device copies."""
@@ -112,6 +133,7 @@ class DeviceTasks:
             if nc:
                 self.d_chunks[: nc * 24].copy_(self.h_chunks[: nc * 24], non_blocking=True)
         self.na, self.nb, self.nc = na, nb, nc
+        self.n_lane_chunks = int(plan.lane_chunks)
 
 
 class PersistentEngine:
@@ -134,6 +156,9 @@ class PersistentEngine:
         self.chunk_bytes = chunk_bytes
         self.can_chunk = np.array([k is Kind.NFA and d.speculative and c.speculate
                                    for k, d, c in zip(self.kinds, self.dev, choices)], dtype=bool)
+        self.lane_ok = np.array([bool(self.can_chunk[i]) and c.lanes and d.lanes and
+                                 d.pair_mean <= LANE_PAIR_MEAN
+                                 for i, (d, c) in enumerate(zip(self.dev, choices))], dtype=bool)
         caps = [c.list_capacity for c, k in zip(choices, self.kinds) if k is Kind.NFA]
         cap = list_capacity if list_capacity else (max(caps) if caps else 32)
         self.max_words = max([d.num_words for d in self.dev if isinstance(d, DeviceNFA)] or [1])
@@ -170,9 +195,10 @@ class PersistentEngine:
 
     # ---- task queue ---------------------------------------------------------------------
 
-    def auto_chunk_bytes(self, nfa_bytes: int) -> int:
-        """Chunk size giving each resident warp about four chunks of the NFA bytes."""
-        per = nfa_bytes // max(1, 4 * self.resident_warps)
+    def auto_chunk_bytes(self, nfa_bytes: int, per_warp: int = 1) -> int:
+        """Chunk size giving each resident chain (warp, or lane when ``per_warp`` is 32)
+        about four chunks of the NFA bytes (a power of two in [MIN_CHUNK, 1 MiB])."""
+        per = nfa_bytes // max(1, 4 * self.resident_warps * per_warp)
         size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
         return int(min(size, 1 << 20))
 
@@ -198,14 +224,21 @@ class PersistentEngine:
         dfa_idx = dfa_idx[np.lexsort((-lengths[dfa_idx], aut_ids[dfa_idx]))]
         input_ids = np.concatenate([nfa_idx, dfa_idx]).astype(np.int32)
         rows = []
-        # NFA inputs: whole, or chunked when long and the automaton allows speculation
-        chunk = 0
+        # NFA inputs: whole, or chunked when long and the automaton allows speculation;
+        # chunks of automata with small two-byte supersets run one per lane
+        lane_in = self.lane_ok[aut_ids] & ~is_dfa
+        warp_in = self.can_chunk[aut_ids] & ~lane_in & ~is_dfa
+        csize = np.zeros(n, dtype=np.int64)
+        chunk_w = chunk_l = 0
         if self.chunk_bytes is not None and nfa_idx.size:
-            chunk = self.chunk_bytes or self.auto_chunk_bytes(int(lengths[nfa_idx].sum()))
-            chunk = max(int(chunk), MIN_CHUNK)
-        split = np.zeros(n, dtype=bool)
-        if chunk:
-            split[nfa_idx] = (lengths[nfa_idx] >= 2 * chunk) & self.can_chunk[aut_ids[nfa_idx]]
+            if self.chunk_bytes:
+                chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
+            else:
+                chunk_w = self.auto_chunk_bytes(int(lengths[warp_in].sum()))
+                chunk_l = self.auto_chunk_bytes(int(lengths[lane_in].sum()), LANE_GROUP)
+            csize[warp_in] = chunk_w
+            csize[lane_in] = chunk_l
+        split = (csize > 0) & (lengths >= 2 * np.maximum(csize, 1))
         whole = nfa_idx[~split[nfa_idx]]
         pos_of = np.empty(n, dtype=np.int64)
         pos_of[nfa_idx] = np.arange(nfa_idx.size)
@@ -213,24 +246,50 @@ class PersistentEngine:
                               np.full_like(whole, native.TASK_WHOLE),
                               lengths[whole] * NFA_BYTE_WEIGHT], axis=1))
         chunk_list, fix_rows = [], []
+        n_lane = 0
         if split.any():
-            sidx = np.flatnonzero(split)
-            counts = lengths[sidx] // chunk  # the last chunk absorbs the remainder
+            # lane-chunked inputs first (grouped by automaton), then warp-chunked ones
+            sl = np.flatnonzero(split & lane_in)
+            sl = sl[np.argsort(aut_ids[sl], kind="stable")]
+            sw = np.flatnonzero(split & ~lane_in)
+            sidx = np.concatenate([sl, sw])
+            cs = csize[sidx]
+            counts = lengths[sidx] // cs  # the last chunk absorbs the remainder
             first = np.zeros(sidx.size, dtype=np.int64)
             np.cumsum(counts[:-1], out=first[1:])
             total = int(counts.sum())
             ch = np.zeros(total, dtype=native.CHUNK_DTYPE)
             inp = np.repeat(sidx, counts)
             idx = np.arange(total) - np.repeat(first, counts)
+            csz = np.repeat(cs, counts)
             ch["input"] = inp
             ch["index"] = idx
-            ch["begin"] = starts[inp] + idx * chunk
+            ch["begin"] = starts[inp] + idx * csz
             last = idx == np.repeat(counts - 1, counts)
-            ch["end"] = np.where(last, starts[inp] + lengths[inp], ch["begin"] + chunk)
+            ch["end"] = np.where(last, starts[inp] + lengths[inp], ch["begin"] + csz)
             chunk_list.append(ch)
-            rows.append(np.stack([aut_ids[inp], np.arange(total), np.ones(total, np.int64),
-                                  np.full(total, native.TASK_CHUNK),
-                                  (ch["end"] - ch["begin"]) * NFA_BYTE_WEIGHT], axis=1))
+            n_lane = int(counts[:sl.size].sum())
+            clen = ch["end"] - ch["begin"]
+            # LANES tasks: up to 32 consecutive lane chunks of one automaton
+            if n_lane:
+                la = aut_ids[inp[:n_lane]]
+                seg = np.flatnonzero(np.r_[True, la[1:] != la[:-1]])
+                seg_end = np.r_[seg[1:], n_lane]
+                g0, gc = [], []
+                for s0, e0 in zip(seg.tolist(), seg_end.tolist()):
+                    for g in range(s0, e0, LANE_GROUP):
+                        g0.append(g)
+                        gc.append(min(LANE_GROUP, e0 - g))
+                g0 = np.asarray(g0, dtype=np.int64)
+                gc = np.asarray(gc, dtype=np.int64)
+                gmax = np.maximum.reduceat(clen[:n_lane], g0)
+                rows.append(np.stack([la[g0], g0, gc, np.full(g0.size, native.TASK_LANES),
+                                      gmax * NFA_BYTE_WEIGHT], axis=1))
+            wc = np.arange(n_lane, total)
+            if wc.size:
+                rows.append(np.stack([aut_ids[inp[wc]], wc, np.ones(wc.size, np.int64),
+                                      np.full(wc.size, native.TASK_CHUNK),
+                                      clen[wc] * NFA_BYTE_WEIGHT], axis=1))
             fix_rows.append(np.stack([aut_ids[sidx], first, counts,
                                       np.full(sidx.size, native.TASK_FIXUP), counts], axis=1))
         if dfa_idx.size:
@@ -254,7 +313,8 @@ class PersistentEngine:
             f = empty
         chunks = np.concatenate(chunk_list) if chunk_list else no_chunks
         return TaskPlan(np.ascontiguousarray(t, dtype=np.int32),
-                        np.ascontiguousarray(f, dtype=np.int32), input_ids, chunks, chunk)
+                        np.ascontiguousarray(f, dtype=np.int32), input_ids, chunks, chunk_w,
+                        n_lane, chunk_l)
 
     # ---- launches -------------------------------------------------------------------------
 
@@ -263,13 +323,13 @@ class PersistentEngine:
         return torch.zeros(self.ws_bytes, dtype=torch.uint8, device=self.device)
 
     def _run(self, tasks_ptr, n_tasks, dt: DeviceTasks, data_ptr, d_off, d_ends, d_flags, d_lens,
-             d_examined, ws, stream) -> None:
+             d_examined, ws, stream, overflow_pass: bool = False) -> None:
+        io = dt.chunk_io(overflow_pass)
         st = native.lib().gbfsm_persistent_run(
             self.table.data_ptr(), len(self.automata), self.max_words, tasks_ptr, int(n_tasks),
             dt.d_ids.data_ptr(), data_ptr, d_off.data_ptr(),
             d_ends.data_ptr() if d_ends is not None else None,
-            dt.d_chunks.data_ptr() if dt.nc else None,
-            dt.d_records.data_ptr() if dt.nc else None,
+            ctypes.byref(io) if dt.nc else None,
             d_flags.data_ptr(), d_lens.data_ptr(),
             d_examined.data_ptr() if d_examined is not None else None,
             ws.data_ptr(), self.ws_bytes, ctypes.byref(self.plan), stream.cuda_stream)
@@ -285,13 +345,21 @@ class PersistentEngine:
         ws = self.workspace if workspace is None else workspace
         data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
         base = dt.d_tasks.data_ptr()
+        launches = 1
+        if dt.n_lane_chunks:
+            with torch.cuda.stream(stream):
+                dt.d_overflow_count.zero_()
         self._run(base, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens, d_examined, ws,
                   stream)
+        if dt.n_lane_chunks:  # chunks that outgrew their lane, run by warps
+            self._run(dt.d_overflow.data_ptr(), dt.n_lane_chunks, dt, data_ptr, d_off, d_ends,
+                      d_flags, d_lens, d_examined, ws, stream, overflow_pass=True)
+            launches += 1
         if dt.nb:
             self._run(base + dt.na * 16, dt.nb, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
                       d_examined, ws, stream)
-            return 2
-        return 1
+            launches += 1
+        return launches
 
     def run_requests(self, aut_ids, inputs, with_examined: bool = False):
         """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``.

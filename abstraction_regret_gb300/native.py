@@ -55,6 +55,9 @@ class NfaDev(ctypes.Structure):
         ("num_eps_edges", ctypes.c_uint64),
         ("first_row", ctypes.c_void_p),
         ("first_edges", ctypes.c_void_p),
+        ("edge_sym", ctypes.c_void_p),
+        ("pair_row", ctypes.c_void_p),
+        ("pair_edges", ctypes.c_void_p),
     ]
 
 
@@ -102,7 +105,14 @@ class Chunk(ctypes.Structure):
                 ("begin", ctypes.c_int64), ("end", ctypes.c_int64)]
 
 
-TASK_WHOLE, TASK_CHUNK, TASK_FIXUP = 0, 1, 2
+class ChunkIO(ctypes.Structure):
+    _fields_ = [("chunks", ctypes.c_void_p), ("records", ctypes.c_void_p),
+                ("overflow_tasks", ctypes.c_void_p), ("overflow_count", ctypes.c_void_p),
+                ("task_count", ctypes.c_void_p)]
+
+
+TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES = 0, 1, 2, 3
+LANE_CAPACITY = 8  # members a lane holds (kLaneCap)
 CHUNK_RECORD_BYTES = 192
 CHUNK_DTYPE = [("input", "<i4"), ("index", "<i4"), ("begin", "<i8"), ("end", "<i8")]
 
@@ -127,8 +137,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_dfa_run": (ctypes.c_int, [_P(DfaDev), _vp, _vp, _i32, _P(Plan), _vp, _vp, _vp, _vp]),
     "gbfsm_persistent_workspace_bytes": (_sz, [_i32, _P(Plan)]),
     "gbfsm_persistent_ctas_per_sm": (_i32, [_i32, _P(Plan)]),
-    "gbfsm_persistent_run": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
-                                            _vp, _vp, _vp, _vp, _vp, _sz, _P(Plan), _vp]),
+    "gbfsm_persistent_run": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _vp, _vp,
+                                            _P(ChunkIO), _vp, _vp, _vp, _vp, _sz, _P(Plan), _vp]),
     "gbfsm_run_multistream": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_shared": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),
     "gbfsm_run_multistream_async": (ctypes.c_int, [_vp] * 8 + [_i32] * 4 + [_vp] * 3),

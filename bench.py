@@ -353,13 +353,13 @@ def main(argv=None) -> int:
     algo = gate.get("examined_bytes", examined_bytes) + 16 * gate.get("edges_scanned", 0) + \
         12 * batch.n_inputs
     achieved = algo / (ms * 1e-3) / 1e9
-    traffic = None
-    tpath = REPO / "profiles" / "traffic.json"
+    traffic = None  # DRAM bytes per launch from the committed ncu summary, when one exists
+    tpath = REPO / "profiles" / "traffic.txt"
     if tpath.exists():
-        try:
-            traffic = json.loads(tpath.read_text()).get(f"persistent_kernel/{args.workload}")
-        except ValueError:
-            traffic = None
+        for line in tpath.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == "persistent_kernel" and parts[1] == args.workload:
+                traffic = int(parts[2])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",

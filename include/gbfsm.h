@@ -94,6 +94,14 @@ typedef struct gbfsm_nfa_dev {
      * makes them a safe starting superset for a chunk that begins mid-input. */
     const uint32_t *first_row;
     const gbfsm_edge *first_edges;
+    /* Optional (NULL = no lane-per-chunk speculation): the label of every symbol edge as
+     * uint16 (0..256), read to filter a state's edges before loading their records; and,
+     * for automata without epsilon edges, the two-byte supersets: for bytes c1, c2 the
+     * distinct states reachable from any state by c1 then c2, as state records
+     * pair_edges[pair_row[c1*256 + c2] .. pair_row[c1*256 + c2 + 1]) (65537 entries). */
+    const uint16_t *edge_sym;
+    const uint32_t *pair_row;
+    const gbfsm_edge *pair_edges;
 } gbfsm_nfa_dev;
 
 /* A DFA on the device. table[s * 256 + c] holds the successor of s on byte c in the low
@@ -202,7 +210,10 @@ typedef struct gbfsm_automaton {
     gbfsm_dfa_dev dfa;     /* valid when kind == 1 */
 } gbfsm_automaton;
 
-/* One task. kind GBFSM_TASK_WHOLE: `count` inputs of automaton `automaton`, whose input
+/* One task. kind GBFSM_TASK_LANES: up to 32 chunks of one automaton, each simulated by a
+ * single lane with a small register-resident set (the automaton needs edge_sym and
+ * pair_row); a chunk whose set outgrows the lane is appended as a CHUNK task to the
+ * overflow queue of gbfsm_chunk_io. kind GBFSM_TASK_WHOLE: `count` inputs of automaton `automaton`, whose input
  * indices are input_ids[first .. first + count); an NFA task has count 1 (a warp runs it),
  * a DFA task 1..32 inputs (one lane each). kind GBFSM_TASK_CHUNK: chunk `first` of the
  * chunk table, simulated speculatively (or exactly when it is an input's first chunk);
@@ -219,6 +230,7 @@ typedef struct gbfsm_task {
 #define GBFSM_TASK_WHOLE 0
 #define GBFSM_TASK_CHUNK 1
 #define GBFSM_TASK_FIXUP 2
+#define GBFSM_TASK_LANES 3 /* chunks[first .. first + count), count <= 32, one per lane */
 
 /* A piece of an NFA input: bytes data[begin .. end) of input `input`; `index` counts the
  * input's chunks from 0. Chunks after the first must start at least 2 bytes into the
@@ -233,12 +245,25 @@ typedef struct gbfsm_chunk {
 /* Bytes of one chunk record (device scratch written by CHUNK tasks, read by FIXUP). */
 #define GBFSM_CHUNK_RECORD_BYTES 192
 
+/* Device buffers of the speculative-chunk machinery (all device pointers; passed by
+ * host pointer, NULL when a launch has no CHUNK, LANES or FIXUP task). */
+typedef struct gbfsm_chunk_io {
+    const gbfsm_chunk *chunks;    /* chunk table */
+    void *records;                /* GBFSM_CHUNK_RECORD_BYTES per chunk */
+    gbfsm_task *overflow_tasks;   /* LANES tasks append CHUNK tasks here (capacity: chunks) */
+    int32_t *overflow_count;      /* entries of overflow_tasks; the caller zeroes it before
+                                     the launch that runs LANES tasks */
+    const int32_t *task_count;    /* non-NULL: run min(*task_count, n_tasks) tasks, a count
+                                     written on the device by an earlier launch */
+} gbfsm_chunk_io;
+
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan);
 
-/* Run `n_tasks` tasks. table/tasks/input_ids (and chunks/chunk_records, needed only by
- * CHUNK and FIXUP tasks) are device arrays. Speculative chunking takes two calls on one
- * stream: the CHUNK tasks (with any WHOLE tasks), then the FIXUP tasks. Input i is
+/* Run `n_tasks` tasks. table/tasks/input_ids (and the chunk_io buffers, needed only by
+ * CHUNK, LANES and FIXUP tasks) are device arrays. Speculative chunking takes up to three
+ * calls on one stream: the LANES / CHUNK tasks (with any WHOLE tasks); the overflow queue
+ * (tasks = overflow_tasks, task_count = overflow_count); then the FIXUP tasks. Input i is
  * data[offsets[i] .. ends[i]) when `ends` is non-NULL (spans anywhere in `data`, e.g.
  * requests left in place in a pinned host pool that the device reads directly), else
  * data[offsets[i] .. offsets[i+1]). Results are written by input index. workspace
@@ -249,9 +274,9 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
                                   int32_t max_words, const gbfsm_task *tasks, int32_t n_tasks,
                                   const int32_t *input_ids, const uint8_t *data,
                                   const int64_t *offsets, const int64_t *ends,
-                                  const gbfsm_chunk *chunks, void *chunk_records, int32_t *flags,
-                                  int32_t *lens, int32_t *examined, void *workspace,
-                                  size_t workspace_bytes, const gbfsm_plan *plan, void *stream);
+                                  const gbfsm_chunk_io *chunk_io, int32_t *flags, int32_t *lens,
+                                  int32_t *examined, void *workspace, size_t workspace_bytes,
+                                  const gbfsm_plan *plan, void *stream);
 
 /* Device address of page-locked host memory (cudaHostGetDevicePointer), for kernels that
  * read request bytes in place over the host link instead of copying them first. No

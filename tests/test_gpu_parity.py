@@ -283,9 +283,17 @@ def test_chunked_persistent_with_epsilon_and_wildcards():
 
 
 @pytest.mark.parametrize("variant", ["live", "sustained"])
-def test_c3_chunked_small_chunks(variant):
+@pytest.mark.parametrize("lanes", [True, False])
+def test_c3_chunked_small_chunks(variant, lanes):
+    """Lane chunks (with sets that outgrow a lane spilling to warps) and warp chunks."""
+    from abstraction_regret_gb300.engine import NfaChoice
+
     b = W.c3(variant, n_inputs=256)
-    eng = PersistentEngine(b.automata, chunk_bytes=512)
+    eng = PersistentEngine(b.automata, chunk_bytes=512, choices=[NfaChoice(lanes=lanes)])
+    plan = eng.make_tasks(b.aut_ids, np.diff(b.offsets))
+    assert (plan.lane_chunks > 0) == lanes
     f, l, e, _, _ = eng.run_requests(b.aut_ids, b.inputs(), with_examined=True)
     of, ol, oe, _ = O.nfa_batch(b.automata[0], b.data, b.offsets)
     assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
+    if lanes:  # some two-byte supersets exceed a lane: the overflow path ran too
+        assert int(eng._tasks.d_overflow_count[0].item()) > 0
