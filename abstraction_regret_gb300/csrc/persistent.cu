@@ -235,7 +235,8 @@ __device__ Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratc
 // of a speculative chunk starts from the two-byte superset pair_edges of the bytes
 // before it; each step scans a member's edge labels (edge_sym, uint16) and loads the
 // 16-byte record only of an edge that matches.
-constexpr int kLaneCap = 8;
+constexpr int kLaneCap = 8;    // members a lane holds
+constexpr int kLaneMatch = 8;  // matching edges a lane handles per byte
 
 __device__ bool run_chunk_lane(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b, int64_t e,
                                int index, ChunkRecord *rec) {
@@ -288,34 +289,60 @@ __device__ bool run_chunk_lane(const gbfsm_nfa_dev &A, const uint8_t *base, int6
     while (!stopped && j < len) {
         const uint32_t sym = bytes.next();
         ++j;
+        // 1. scan the members' edge labels (L1-resident uint16) for this byte, keeping the
+        //    indices of at most kLaneMatch matching edges
+        uint32_t mk[kLaneMatch];
+        int nm = 0;
+#pragma unroll
+        for (int q = 0; q < kLaneMatch; ++q) mk[q] = 0;
+#pragma unroll
+        for (int i = 0; i < kLaneCap; ++i) {
+            if (i < m) {
+                const uint32_t kb = crb[i], ke = cre[i];
+#pragma unroll 4
+                for (uint32_t k = kb; k < ke; ++k) {
+                    const uint32_t es = __ldg(A.edge_sym + k);
+                    if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) {
+#pragma unroll
+                        for (int q = 0; q < kLaneMatch; ++q)
+                            if (q == nm) mk[q] = k;
+                        ++nm;
+                    }
+                }
+            }
+        }
+        if (nm > kLaneMatch) return false;
+        // 2. load the matching edges' records together (one L2 round trip per byte)
+        uint4 rr[kLaneMatch];
+#pragma unroll
+        for (int q = 0; q < kLaneMatch; ++q)
+            rr[q] = (q < nm) ? ld_edge(A.sym_edges + mk[q]) : make_uint4(0, 0, 0, 0);
+        // 3. deduplicate the targets into the next set
         uint32_t nt[kLaneCap], nrb[kLaneCap], nre[kLaneCap];
         int n = 0;
         bool acc = false, ovf = false;
 #pragma unroll
-        for (int i = 0; i < kLaneCap; ++i) {
-            if (i < m) {
-                for (uint32_t k = crb[i]; k < cre[i]; ++k) {
-                    const uint32_t es = __ldg(A.edge_sym + k);
-                    if (es != sym && es != (uint32_t)GBFSM_ANY_SYMBOL) continue;
-                    const uint4 r = ld_edge(A.sym_edges + k);
-                    bool dup = false;
+        for (int q = 0; q < kLaneMatch; ++q) {
+            if (q < nm) {
+                const uint4 r = rr[q];
+                bool dup = false;
 #pragma unroll
-                    for (int q = 0; q < kLaneCap; ++q) dup |= (q < n) && (nt[q] == r.x);
-                    if (dup) continue;
+                for (int u = 0; u < q; ++u) dup |= (rr[u].x == r.x);
+                if (!dup) {
                     if (n == kLaneCap) {
                         ovf = true;
-                        continue;
-                    }
+                    } else {
 #pragma unroll
-                    for (int q = 0; q < kLaneCap; ++q) {
-                        if (q == n) {
-                            nt[q] = r.x;
-                            nrb[q] = r.z;
-                            nre[q] = r.w;
+                        for (int u = 0; u < kLaneCap; ++u) {
+                            if (u == n) {
+                                nt[u] = r.x;
+                                nrb[u] = r.z;
+                                nre[u] = r.w;
+                            }
                         }
+                        ++n;
+                        acc |= (r.y & GBFSM_EDGE_ACCEPT) != 0;
                     }
-                    ++n;
-                    acc |= (r.y & GBFSM_EDGE_ACCEPT) != 0;
                 }
             }
         }

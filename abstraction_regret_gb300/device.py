@@ -209,7 +209,8 @@ class DeviceNFA:
             d.first_edges = self.first_edges.data_ptr()
         pairs = pair_lists(nfa, lists)
         self.lanes = pairs is not None
-        self.pair_mean = float(np.diff(pairs[0]).mean()) if pairs is not None else float("inf")
+        self.pair_sizes = np.diff(pairs[0]).astype(np.int32) if pairs is not None else None
+        self.pair_mean = float(self.pair_sizes.mean()) if pairs is not None else float("inf")
         if pairs is not None:
             prow, precs = pairs
             with torch.cuda.device(dev):

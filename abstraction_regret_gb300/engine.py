@@ -49,6 +49,10 @@ LANE_GROUP = 32      # chunks per LANES task (one per lane)
 # an automaton's chunks run one per lane when its two-byte supersets are this small on
 # average (the lane holds at most native.LANE_CAPACITY states; larger sets spill to warps)
 LANE_PAIR_MEAN = 4.0
+# a lane chunk's start is moved forward (by less than BOUNDARY_WINDOW bytes) to the first
+# position whose two-byte superset has at most BOUNDARY_SET states, when one exists
+BOUNDARY_WINDOW = 32
+BOUNDARY_SET = 4
 
 
 @dataclass
@@ -202,9 +206,33 @@ class PersistentEngine:
         size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
         return int(min(size, 1 << 20))
 
-    def make_tasks(self, aut_ids, lengths, starts=None) -> TaskPlan:
+    def _shift_boundaries(self, ch: np.ndarray, inp: np.ndarray, aut: np.ndarray,
+                          data: np.ndarray) -> None:
+        """Move the start of every non-first lane chunk (and the end of its predecessor)
+        forward to the first position in the next BOUNDARY_WINDOW bytes whose two-byte
+        superset holds at most BOUNDARY_SET states (the smallest one if none does): a
+        smaller starting superset converges sooner and rarely outgrows the lane."""
+        later = np.flatnonzero(ch["index"] > 0)
+        if later.size == 0:
+            return
+        span = (ch["end"][later] - ch["begin"][later]).min()
+        w = int(min(BOUNDARY_WINDOW, max(1, span // 4)))
+        for a in np.unique(aut[later]):
+            sizes = self.dev[int(a)].pair_sizes
+            sel = later[aut[later] == a]
+            pos = ch["begin"][sel][:, None] + np.arange(w)[None, :]
+            key = data[pos - 2].astype(np.int64) * 256 + data[pos - 1]
+            sz = sizes[key]
+            ok = sz <= BOUNDARY_SET
+            pick = np.where(ok.any(axis=1), ok.argmax(axis=1), sz.argmin(axis=1))
+            new_begin = ch["begin"][sel] + pick
+            ch["begin"][sel] = new_begin
+            ch["end"][sel - 1] = new_begin
+
+    def make_tasks(self, aut_ids, lengths, starts=None, data=None) -> TaskPlan:
         """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
-        packed back to back from 0) on automaton ``aut_ids[i]``."""
+        packed back to back from 0) on automaton ``aut_ids[i]``. ``data`` (host bytes,
+        indexed like ``starts``) lets lane chunks start where the superset is small."""
         aut_ids = np.asarray(aut_ids, dtype=np.int64)
         lengths = np.asarray(lengths, dtype=np.int64)
         n = aut_ids.size
@@ -267,8 +295,11 @@ class PersistentEngine:
             ch["begin"] = starts[inp] + idx * csz
             last = idx == np.repeat(counts - 1, counts)
             ch["end"] = np.where(last, starts[inp] + lengths[inp], ch["begin"] + csz)
-            chunk_list.append(ch)
             n_lane = int(counts[:sl.size].sum())
+            if n_lane and data is not None:
+                self._shift_boundaries(ch[:n_lane], inp[:n_lane], aut_ids[inp[:n_lane]],
+                                       np.asarray(data))
+            chunk_list.append(ch)
             clen = ch["end"] - ch["begin"]
             # LANES tasks: up to 32 consecutive lane chunks of one automaton
             if n_lane:
@@ -371,8 +402,8 @@ class PersistentEngine:
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
         lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
-        plan = self.make_tasks(np.asarray(aut_ids), lengths)
         d_data, d_off, _, _ = self._staging.put(inputs, stream)
+        plan = self.make_tasks(np.asarray(aut_ids), lengths, data=self._staging.host_data())
         self._tasks.upload(plan, stream)
         self._results.ensure(max(n, 1))
         res = self._results
@@ -418,7 +449,8 @@ class GraphRunner:
         n = len(offsets) - 1
         self.n = n
         lengths = np.diff(np.asarray(offsets, dtype=np.int64))
-        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths)
+        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths,
+                                           data=np.asarray(data, dtype=np.uint8))
         total = int(offsets[-1])
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
