@@ -145,8 +145,9 @@ class PersistentEngine:
 
     def __init__(self, automata, device=None, choices=None, block_threads: int = 256,
                  list_capacity: int | None = None, ctas_per_sm: int = 0,
-                 chunk_bytes: int | None = 0) -> None:
-        """``chunk_bytes``: 0 = chosen per batch, None = never chunk, else a fixed size."""
+                 chunk_bytes: int | None = 0, lane_pair_mean: float = LANE_PAIR_MEAN) -> None:
+        """``chunk_bytes``: 0 = chosen per batch, None = never chunk, else a fixed size.
+        ``lane_pair_mean``: largest mean two-byte superset for one-lane-per-chunk tasks."""
         self.device = resolve_device(device)
         self.automata = list(automata)
         if not self.automata:
@@ -161,7 +162,7 @@ class PersistentEngine:
         self.can_chunk = np.array([k is Kind.NFA and d.speculative and c.speculate
                                    for k, d, c in zip(self.kinds, self.dev, choices)], dtype=bool)
         self.lane_ok = np.array([bool(self.can_chunk[i]) and c.lanes and d.lanes and
-                                 d.pair_mean <= LANE_PAIR_MEAN
+                                 d.pair_mean <= lane_pair_mean
                                  for i, (d, c) in enumerate(zip(self.dev, choices))], dtype=bool)
         caps = [c.list_capacity for c, k in zip(choices, self.kinds) if k is Kind.NFA]
         cap = list_capacity if list_capacity else (max(caps) if caps else 32)

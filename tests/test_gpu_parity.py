@@ -295,5 +295,18 @@ def test_c3_chunked_small_chunks(variant, lanes):
     f, l, e, _, _ = eng.run_requests(b.aut_ids, b.inputs(), with_examined=True)
     of, ol, oe, _ = O.nfa_batch(b.automata[0], b.data, b.offsets)
     assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
-    if lanes:  # some two-byte supersets exceed a lane: the overflow path ran too
-        assert int(eng._tasks.d_overflow_count[0].item()) > 0
+
+
+def test_lane_chunks_that_outgrow_the_lane_fall_back_to_warps():
+    """High out-degree: sets exceed a lane's capacity, so chunks take the overflow path."""
+    nfa = W.random_nfa(1500, seed=11, poisson=20.0, accept_prob=0.0005)
+    lengths = W.log_uniform_lengths(np.random.default_rng(3), 96, 2000, 20000)
+    off = W.offsets_of(lengths)
+    data = W.walk_bytes(nfa, off, seed=4)
+    inputs = [data[off[i]:off[i + 1]].tobytes() for i in range(lengths.size)]
+    eng = PersistentEngine([nfa], chunk_bytes=512, lane_pair_mean=float("inf"))
+    assert eng.make_tasks(np.zeros(lengths.size), lengths).lane_chunks > 0
+    f, l, e, _, _ = eng.run_requests(np.zeros(lengths.size), inputs, with_examined=True)
+    assert int(eng._tasks.d_overflow_count[0].item()) > 0
+    of, ol, oe, _ = O.nfa_batch(nfa, data, off)
+    assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
