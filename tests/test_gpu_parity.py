@@ -298,8 +298,14 @@ def test_c3_chunked_small_chunks(variant, lanes):
 
 
 def test_lane_chunks_that_outgrow_the_lane_fall_back_to_warps():
-    """High out-degree: sets exceed a lane's capacity, so chunks take the overflow path."""
-    nfa = W.random_nfa(1500, seed=11, poisson=20.0, accept_prob=0.0005)
+    """Wildcard edges keep sets above a lane's capacity: chunks take the overflow path."""
+    rng = np.random.default_rng(11)
+    n, deg = 400, 3
+    syms = np.where(rng.random(n * deg) < 0.06, G.ANY_SYMBOL, rng.integers(0, 256, n * deg))
+    accept = rng.random(n) < 0.002
+    accept[0] = False
+    nfa = G.nfa_from_edges(n, 0, accept, np.repeat(np.arange(n), deg), syms,
+                           rng.integers(0, n, n * deg))
     lengths = W.log_uniform_lengths(np.random.default_rng(3), 96, 2000, 20000)
     off = W.offsets_of(lengths)
     data = W.walk_bytes(nfa, off, seed=4)
