@@ -223,6 +223,19 @@ gbfsm_status gbfsm_host_device_pointer(void *host, void **device) {
     return GBFSM_OK;
 }
 
+gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
+                             const gbfsm_task *tasks, int32_t n_tasks, const uint8_t *data,
+                             const int64_t *offsets, const gbfsm_chunk_io *chunk_io,
+                             void *stream) {
+    if (n_tasks < 0 || n_automata < 0) return fail(GBFSM_INVALID_ARG, "negative task count");
+    if (n_tasks == 0) return GBFSM_OK;
+    if (!table || !tasks || !data || !offsets || !chunk_io || !chunk_io->chunks ||
+        !chunk_io->records || !chunk_io->overflow_tasks || !chunk_io->overflow_count)
+        return fail(GBFSM_INVALID_ARG, "NULL array passed to gbfsm_lanes_run");
+    return launch_lanes(table, tasks, n_tasks, data, offsets, *chunk_io,
+                        static_cast<cudaStream_t>(stream));
+}
+
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan) {
     const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
     return persistent_workspace_bytes(max_words, p);

@@ -1,0 +1,524 @@
+// Speculative chunk-parallel NFA simulation: the chunk record, the warp and lane chunk
+// runners and the exact fix-up (shared by persistent.cu and lanes.cu).
+//
+// An input is cut into chunks. Its first chunk runs exactly from the start configuration.
+// Every later chunk starting at byte b runs from a superset of the true active set at b:
+// the targets of every edge labelled x[b-2] (or ANY), stepped over x[b-1] (for automata
+// without epsilon edges this two-byte superset is tabulated, pair_edges). Because
+// simulation preserves set inclusion, the speculative set contains the true set at every
+// later position of the chunk, so equal sizes mean equal sets. The chunk records its set
+// sizes after 1, 2, 4, ..., 32 bytes, the first accept strictly after each of those
+// checkpoints, where it died, and its final set; it then continues its run up to 32 bytes
+// into the next chunk (the overlap) and records that run's sizes and first event.
+//
+// Fix-up. Chunk k is linked to chunk k-1 when, at some checkpoint and before any event of
+// the overlap run, the overlap run of chunk k-1 has the size chunk k recorded. If chunk
+// k-1's run is exact, so is its overlap run, which then equals chunk k's speculative run
+// from that checkpoint on: chunk k's record is exact from there. The first chunk is
+// exact, so along a chain of links every record is exact, and an input's verdict is that
+// of the first chunk that decides (an accept or a death, in its overlap prefix or its
+// record). The fix-up is therefore a warp-parallel scan over the chunks; only at a chunk
+// that cannot be linked does it fall back to re-running chunks serially from the last
+// exact recorded set, checking sizes at the checkpoints the same way. Verdicts are
+// exactly those of a serial run (src/gpufsm/reference.py:36-65).
+#pragma once
+
+#include "common.cuh"
+#include "nfa_device.cuh"
+
+namespace gbfsm {
+
+constexpr int kCheckpoints = 6;  // set sizes after 1, 2, 4, 8, 16, 32 bytes of a chunk
+constexpr int kOverlap = 1 << (kCheckpoints - 1);  // bytes a run continues into the next chunk
+constexpr int kEndCap = 8;       // states of a chunk's final set kept in its record
+constexpr int kLaneSlots = 4;    // states (and matching edges per byte) a lane handles
+
+// Outcome of one chunk (GBFSM_CHUNK_RECORD_BYTES bytes). Positions are byte counts from
+// the start of the chunk's input. acc_after[c]: first accepting position strictly after
+// checkpoint c (-1: none before the run stopped); dead_at: position at which the run's
+// set became empty (-1: never). For an input's first chunk (exact) acc_after[0] / dead_at
+// are the input's own first accept / death. end_recs: the set at the chunk end as state
+// records, when the run got there with at most kEndCap members (end_count, else -1).
+// The overlap run (from the end set into the next chunk of the same input): ov_len bytes
+// stepped, ov_event = +j / -j when it accepted / died at its j-th byte (0: neither),
+// ov_counts[c] its size after 2^c bytes.
+struct ChunkRecord {
+    int32_t counts[kCheckpoints];
+    int32_t acc_after[kCheckpoints];
+    int32_t dead_at;
+    int32_t end_count;
+    int32_t ov_len;
+    int32_t ov_event;
+    int32_t ov_counts[kCheckpoints];
+    int32_t pad[10];
+    uint4 end_recs[kEndCap];
+};
+static_assert(sizeof(ChunkRecord) == GBFSM_CHUNK_RECORD_BYTES, "chunk record layout");
+
+// Device pointers of the chunk machinery, passed by value to the kernels.
+struct ChunkIO {
+    const gbfsm_chunk *chunks;
+    ChunkRecord *records;
+    gbfsm_task *overflow_tasks;
+    int32_t *overflow_count;
+    const int32_t *task_count;
+    int32_t n_chunks;
+};
+
+// End (input-relative, like b and e) of the overlap run of chunk `cid` ending at e: up to
+// kOverlap bytes into the next chunk when that chunk belongs to the same input.
+__device__ __forceinline__ int64_t overlap_end(const ChunkIO &io, int cid, int64_t e,
+                                               int64_t off) {
+    if (cid + 1 >= io.n_chunks) return e;
+    const gbfsm_chunk nx = io.chunks[cid + 1];
+    if (nx.index == 0) return e;
+    return min(e + (int64_t)kOverlap, nx.end - off);
+}
+
+__device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }
+
+__device__ __forceinline__ int checkpoint_of(int64_t j) {
+    return (j >= 1 && j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) ? 31 - __clz((int)j)
+                                                                            : -1;
+}
+
+// Record an accept at position `pos` (j bytes into a speculative chunk): it is the first
+// accept after every checkpoint before j that has none yet.
+__device__ __forceinline__ void note_accept(int32_t (&acc_after)[kCheckpoints], int64_t j,
+                                            int32_t pos) {
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c)
+        if (j > (1 << c) && acc_after[c] < 0) acc_after[c] = pos;
+}
+
+// ---- warp chunk (any set size; the overflow path of lane chunks) --------------------------
+
+__device__ __forceinline__ void write_overlap(ChunkRecord *rec, int32_t ov_len, int32_t ov_event,
+                                              const int32_t (&ov_counts)[kCheckpoints]) {
+    rec->ov_len = ov_len;
+    rec->ov_event = ov_event;
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) rec->ov_counts[c] = ov_counts[c];
+}
+
+// b, e, ov_end: input-relative bounds of the chunk and of its overlap run.
+__device__ inline void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
+                                 const uint8_t *base, int64_t b, int64_t e, int64_t ov_end,
+                                 int index, ChunkRecord *rec) {
+    const uint32_t lane = lane_id();
+    WarpNfa<false> w(nfa, R, S);
+    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        counts[c] = 0;
+        acc_after[c] = -1;
+    }
+    int32_t dead_at = -1;
+    bool stopped = false;
+    int ev;
+    if (index == 0) {
+        ev = w.init_start();
+        if (ev == kAccept) {
+            acc_after[0] = 0;
+            stopped = true;
+        }
+    } else {
+        const uint32_t c0 = byte_at(base + b - 2);
+        ev = w.init_records(nfa.first_edges, __ldg(nfa.first_row + c0),
+                            __ldg(nfa.first_row + c0 + 1));
+        if (ev != kDead) ev = w.step(byte_at(base + b - 1));
+        if (ev == kDead) {
+            dead_at = (int32_t)b;
+            stopped = true;
+        }
+    }
+    const int64_t len = e - b;
+    ByteStream bytes;
+    bytes.init(base + b, stopped ? 0 : len);
+    int64_t j = 0;
+    while (!stopped && j < len) {
+        ev = w.step(bytes.next());
+        ++j;
+        const int32_t pos = (int32_t)(b + j);
+        if (ev == kDead) {
+            dead_at = pos;
+            stopped = true;
+        } else if (ev == kAccept) {
+            if (index == 0) {
+                acc_after[0] = pos;
+                stopped = true;
+            } else {
+                note_accept(acc_after, j, pos);
+                if (j > kOverlap) stopped = true;
+            }
+        }
+        const int c = checkpoint_of(j);
+        if (c >= 0 && ev != kDead) counts[c] = w.m;
+    }
+    int32_t end_count = -1;
+    int32_t ov_len = 0, ov_event = 0, ov_counts[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) ov_counts[c] = 0;
+    if (!stopped) {
+        end_count = w.export_recs(rec->end_recs, kEndCap);
+        __syncwarp();
+        for (int64_t t = 1; t <= ov_end - e; ++t) {
+            const int ev2 = w.step(byte_at(base + e + t - 1));
+            ov_len = (int32_t)t;
+            if (ev2 == kDead) {
+                ov_event = -(int32_t)t;
+                break;
+            }
+            if (ev2 == kAccept) {
+                ov_event = (int32_t)t;
+                break;
+            }
+            const int c = checkpoint_of(t);
+            if (c >= 0) ov_counts[c] = w.m;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < kCheckpoints; ++c) {
+            rec->counts[c] = counts[c];
+            rec->acc_after[c] = acc_after[c];
+        }
+        rec->dead_at = dead_at;
+        rec->end_count = end_count;
+        write_overlap(rec, ov_len, ov_event, ov_counts);
+    }
+    w.cleanup();
+}
+
+// ---- lane chunk (one chunk per thread; up to kLaneSlots states) ----------------------------
+//
+// The set is kept as the records of its members (slot q valid when bit q of `valid` is
+// set). Per byte: scan the members' edge labels (uint16, L1-resident) for the byte,
+// collecting at most kLaneSlots matching edges; load their records together (one L2 round
+// trip); the deduplicated targets are the next set.
+
+// One byte: returns the new member count (acc: a member accepts), or -1 when more than
+// kLaneSlots edges match.
+__device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
+                                         uint32_t sym, const uint16_t *__restrict__ labels,
+                                         const gbfsm_edge *__restrict__ edges) {
+    uint32_t mk[kLaneSlots];
+    int nm = 0;
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0;
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q) {
+        if ((valid >> q) & 1u) {
+            const uint32_t ke = cur[q].w;
+#pragma unroll 4
+            for (uint32_t k = cur[q].z; k < ke; ++k) {
+                const uint32_t es = __ldg(labels + k);
+                if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) {
+#pragma unroll
+                    for (int u = 0; u < kLaneSlots; ++u)
+                        if (u == nm) mk[u] = k;
+                    ++nm;
+                }
+            }
+        }
+    }
+    if (nm > kLaneSlots) return -1;
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q)
+        cur[q] = (q < nm) ? ld_edge(edges + mk[q]) : make_uint4(0, 0, 0, 0);
+    valid = 0;
+    acc = false;
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q) {
+        bool keep = q < nm;
+#pragma unroll
+        for (int u = 0; u < q; ++u) keep = keep && (cur[u].x != cur[q].x);
+        if (keep) {
+            valid |= 1u << q;
+            acc |= (cur[q].y & GBFSM_EDGE_ACCEPT) != 0;
+        }
+    }
+    return __popc(valid);
+}
+
+// Returns false, writing nothing, when a start superset or a byte's matches exceed
+// kLaneSlots inside the chunk (the chunk is then run by a warp); in the overlap that only
+// ends the overlap run.
+__device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b,
+                                  int64_t e, int64_t ov_end, int index, ChunkRecord *rec) {
+    uint4 cur[kLaneSlots];
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q) cur[q] = make_uint4(0, 0, 0, 0);
+    uint32_t valid = 0;
+    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        counts[c] = 0;
+        acc_after[c] = -1;
+    }
+    int32_t dead_at = -1;
+    bool stopped = false;
+    if (index == 0) {
+        const uint32_t s = (uint32_t)A.start_state;
+        const bool acc =
+            (__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
+             (s & 63u)) & 1ull;
+        cur[0] = make_uint4(s, acc ? GBFSM_EDGE_ACCEPT : 0u, __ldg(A.sym_row + s),
+                            __ldg(A.sym_row + s + 1));
+        valid = 1;
+        if (acc) {
+            acc_after[0] = 0;
+            stopped = true;
+        }
+    } else {
+        const uint32_t key = byte_at(base + b - 2) * 256u + byte_at(base + b - 1);
+        const uint32_t pr = __ldg(A.pair_row + key);
+        const uint32_t cnt = __ldg(A.pair_row + key + 1) - pr;
+        if (cnt > (uint32_t)kLaneSlots) return false;
+#pragma unroll
+        for (int q = 0; q < kLaneSlots; ++q)
+            if ((uint32_t)q < cnt) cur[q] = ld_edge(A.pair_edges + pr + q);
+        valid = (1u << cnt) - 1u;
+        if (cnt == 0) {
+            dead_at = (int32_t)b;
+            stopped = true;
+        }
+    }
+    const uint16_t *__restrict__ labels = A.edge_sym;
+    const gbfsm_edge *__restrict__ edges = A.sym_edges;
+    const int64_t len = e - b;
+    ByteStream bytes;
+    bytes.init(base + b, stopped ? 0 : len);
+    int64_t j = 0;
+    int m = __popc(valid);
+    while (!stopped && j < len) {
+        const uint32_t sym = bytes.next();
+        ++j;
+        bool acc;
+        m = lane_step(cur, valid, acc, sym, labels, edges);
+        if (m < 0) return false;
+        const int32_t pos = (int32_t)(b + j);
+        if (m == 0) {  // reference.py:59-60
+            dead_at = pos;
+            stopped = true;
+            break;
+        }
+        if (acc) {
+            if (index == 0) {
+                acc_after[0] = pos;
+                stopped = true;
+                break;
+            }
+            note_accept(acc_after, j, pos);
+            if (j > kOverlap) stopped = true;
+        }
+        const int c = checkpoint_of(j);
+#pragma unroll
+        for (int q = 0; q < kCheckpoints; ++q)
+            if (q == c) counts[q] = m;
+    }
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        rec->counts[c] = counts[c];
+        rec->acc_after[c] = acc_after[c];
+    }
+    rec->dead_at = dead_at;
+    rec->end_count = stopped ? -1 : m;
+    int32_t ov_len = 0, ov_event = 0, ov_counts[kCheckpoints];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) ov_counts[c] = 0;
+    if (!stopped) {
+        int o = 0;
+#pragma unroll
+        for (int q = 0; q < kLaneSlots; ++q) {
+            if ((valid >> q) & 1u) {
+                rec->end_recs[o] = cur[q];
+                ++o;
+            }
+        }
+        for (int64_t t = 1; t <= ov_end - e; ++t) {
+            bool acc;
+            const int nm = lane_step(cur, valid, acc, byte_at(base + e + t - 1), labels, edges);
+            if (nm < 0) break;
+            ov_len = (int32_t)t;
+            if (nm == 0) {
+                ov_event = -(int32_t)t;
+                break;
+            }
+            if (acc) {
+                ov_event = (int32_t)t;
+                break;
+            }
+            const int c = checkpoint_of(t);
+#pragma unroll
+            for (int q = 0; q < kCheckpoints; ++q)
+                if (q == c) ov_counts[q] = nm;
+        }
+    }
+    write_overlap(rec, ov_len, ov_event, ov_counts);
+    return true;
+}
+
+// ---- exact fix-up (one warp per chunked input) ----------------------------------------------
+
+struct RecordHead {
+    int32_t counts[kCheckpoints];
+    int32_t acc_after[kCheckpoints];
+    int32_t dead_at;
+    int32_t end_count;
+    int64_t begin;
+    int64_t end;
+};
+
+__device__ __forceinline__ RecordHead load_head(const gbfsm_chunk *chunks,
+                                                const ChunkRecord *recs, int k) {
+    RecordHead h;
+    const ChunkRecord &r = recs[k];
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        h.counts[c] = r.counts[c];
+        h.acc_after[c] = r.acc_after[c];
+    }
+    h.dead_at = r.dead_at;
+    h.end_count = r.end_count;
+    h.begin = chunks[k].begin;
+    h.end = chunks[k].end;
+    return h;
+}
+
+enum LinkStatus { kLink = 0, kDecide = 1, kBreak = 2 };
+
+// Chunk `rk` (starting `begin` bytes into its input) against its predecessor's overlap
+// run: kLink (its record is exact from a checkpoint on and has no event), kDecide (the
+// input's verdict: accept when flag, at / examined up to `pos`), or kBreak (no link).
+__device__ __forceinline__ int classify(const ChunkRecord &prev, const ChunkRecord &rk,
+                                        int64_t begin, int32_t &flag, int64_t &pos) {
+    const int32_t ov_len = prev.ov_len, ov_event = prev.ov_event;
+    const int32_t ov_at = ov_event < 0 ? -ov_event : ov_event;
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        const int32_t j = 1 << c;
+        if (ov_event != 0 && ov_at <= j) {
+            flag = ov_event > 0;
+            pos = begin + ov_at;
+            return kDecide;
+        }
+        if (j > ov_len) return kBreak;
+        if (prev.ov_counts[c] == rk.counts[c]) {
+            if (rk.acc_after[c] >= 0) {
+                flag = 1;
+                pos = rk.acc_after[c];
+                return kDecide;
+            }
+            if (rk.dead_at >= 0) {
+                flag = 0;
+                pos = rk.dead_at;
+                return kDecide;
+            }
+            return kLink;
+        }
+    }
+    return kBreak;
+}
+
+__device__ __forceinline__ Verdict decided(int32_t flag, int64_t pos) {
+    Verdict v;
+    v.flag = flag;
+    v.len = flag ? (int32_t)pos : 0;
+    v.examined = pos;
+    return v;
+}
+
+// Serial re-run of chunks [start, count) from the exact set already in `w`; the part of
+// the fix-up that runs only from a chunk the scan could not link.
+__device__ inline Verdict serial_fixup(WarpNfa<false> &w, const uint8_t *base, int64_t len,
+                                       const gbfsm_chunk *chunks, const ChunkRecord *recs,
+                                       int first, int start, int count, int64_t input_off) {
+    Verdict v{0, 0, len};
+    RecordHead next = load_head(chunks, recs, first + start);
+    for (int k = start; k < count; ++k) {
+        const RecordHead rk = next;
+        if (k + 1 < count) next = load_head(chunks, recs, first + k + 1);  // prefetch
+        const int64_t b = rk.begin - input_off, e = rk.end - input_off;
+        int matched = -1;
+        int64_t j = 0;
+        while (b + j < e) {
+            const int ev = w.step(byte_at(base + b + j));
+            ++j;
+            if (ev == kDead) return decided(0, b + j);
+            if (ev == kAccept) return decided(1, b + j);
+            const int c = checkpoint_of(j);
+            if (c >= 0 && w.m == rk.counts[c]) {
+                matched = c;
+                break;
+            }
+        }
+        if (matched >= 0) {
+            if (rk.acc_after[matched] >= 0) return decided(1, rk.acc_after[matched]);
+            if (rk.dead_at >= 0) return decided(0, rk.dead_at);
+            if (rk.end_count >= 0) {
+                w.cleanup();
+                w.init_recs(recs[first + k].end_recs, rk.end_count);
+            } else {
+                while (b + j < e) w.step(byte_at(base + b + j++));  // no event can occur here
+            }
+        }
+    }
+    return v;
+}
+
+__device__ inline Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
+                                    const uint8_t *base, int64_t len, const gbfsm_chunk *chunks,
+                                    const ChunkRecord *recs, int first, int count,
+                                    int64_t input_off) {
+    const uint32_t lane = lane_id();
+    const ChunkRecord &r0 = recs[first];
+    if (r0.acc_after[0] >= 0) return decided(1, r0.acc_after[0]);
+    if (r0.dead_at >= 0) return decided(0, r0.dead_at);
+    // scan: 32 chunks per round, one per lane; stop at the first that is not linked
+    int last_rec = r0.end_count >= 0 ? 0 : -1;  // last chunk with an exact recorded end set
+    int brk = -1;
+    for (int k0 = 1; k0 < count && brk < 0; k0 += 32) {
+        const int k = k0 + (int)lane;
+        int status = kLink;
+        int32_t flag = 0;
+        int64_t pos = 0;
+        bool rec_ok = false;
+        if (k < count) {
+            const ChunkRecord &rk = recs[first + k];
+            status = classify(recs[first + k - 1], rk, chunks[first + k].begin - input_off,
+                              flag, pos);
+            rec_ok = rk.end_count >= 0;
+        }
+        const uint32_t stop = __ballot_sync(GBFSM_FULL_MASK, status != kLink);
+        const uint32_t before = stop ? (stop & (0u - stop)) - 1u : GBFSM_FULL_MASK;
+        const uint32_t recm = __ballot_sync(GBFSM_FULL_MASK, rec_ok) & before;
+        if (recm) last_rec = k0 + 31 - __clz(recm);
+        if (stop) {
+            const int src = __ffs(stop) - 1;
+            status = __shfl_sync(GBFSM_FULL_MASK, status, src);
+            flag = __shfl_sync(GBFSM_FULL_MASK, flag, src);
+            pos = __shfl_sync(GBFSM_FULL_MASK, pos, src);
+            if (status == kDecide) return decided(flag, pos);
+            brk = k0 + src;
+        }
+    }
+    if (brk < 0) return Verdict{0, 0, len};  // every chunk linked, no event: no accept
+    // fall back: serial from the chunk after the last exact recorded end set
+    WarpNfa<false> w(nfa, R, S);
+    int start;
+    if (last_rec >= 0) {
+        w.init_recs(recs[first + last_rec].end_recs, recs[first + last_rec].end_count);
+        start = last_rec + 1;
+    } else {  // the first chunk's final set was not recorded: recompute it exactly
+        w.init_start();
+        const int64_t e0 = chunks[first].end - input_off;
+        for (int64_t p = 0; p < e0; ++p) w.step(byte_at(base + p));
+        start = 1;
+    }
+    const Verdict v = serial_fixup(w, base, len, chunks, recs, first, start, count, input_off);
+    w.cleanup();
+    return v;
+}
+
+}  // namespace gbfsm

@@ -71,6 +71,9 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_chunk_io *chunk_io, int32_t *flags,
                                int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream);
+gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
+                          const uint8_t *data, const int64_t *offsets,
+                          const gbfsm_chunk_io &chunk_io, cudaStream_t stream);
 size_t persistent_workspace_bytes(int32_t max_words, const gbfsm_plan &p);
 int32_t persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan &p);
 gbfsm_status launch_nfa_layout(int32_t n, const int32_t *srp, const int32_t *stg,

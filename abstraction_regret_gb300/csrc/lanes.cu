@@ -1,0 +1,63 @@
+// One-lane-per-chunk speculative NFA launch (GBFSM_TASK_LANES tasks).
+//
+// Each warp takes one LANES task (up to 32 chunks of one automaton) and each lane runs one
+// chunk with lane_chunk() (chunks.cuh): a set of at most kLaneSlots states held as their
+// records in registers, one L1 label scan and one batched L2 record load per byte. A chunk
+// that outgrows its lane is appended to the overflow queue as a CHUNK task, which the
+// persistent launch then runs with a whole warp. The kernel holds no per-warp shared
+// state and no warp-wide loop, so it runs in a separate, lighter launch than the
+// persistent kernel and fits more resident warps per SM.
+#include "chunks.cuh"
+#include "common.cuh"
+#include "engine.hpp"
+
+namespace gbfsm {
+namespace {
+
+constexpr int kLanesThreads = 128;
+#ifndef GBFSM_LANES_MIN_BLOCKS
+#define GBFSM_LANES_MIN_BLOCKS 8
+#endif
+constexpr int kLanesMinBlocks = GBFSM_LANES_MIN_BLOCKS;  // 8 x 128 threads: 64 registers
+
+__global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
+    const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
+    int32_t n_tasks, const uint8_t *__restrict__ data, const int64_t *__restrict__ offsets,
+    ChunkIO io) {
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (warp >= n_tasks) return;
+    const gbfsm_task task = tasks[warp];
+    const int lane = (int)lane_id();
+    if (lane >= task.count) return;
+    const int cid = task.first + lane;
+    const gbfsm_chunk ch = io.chunks[cid];
+    const int64_t off = offsets[ch.input];
+    const gbfsm_nfa_dev &A = table[task.automaton].nfa;
+    const int64_t e = ch.end - off;
+    if (!lane_chunk(A, data + off, ch.begin - off, e, overlap_end(io, cid, e, off), ch.index,
+                    io.records + cid)) {
+        gbfsm_task spill;
+        spill.automaton = task.automaton;
+        spill.first = cid;
+        spill.count = 1;
+        spill.kind = GBFSM_TASK_CHUNK;
+        io.overflow_tasks[atomicAdd(io.overflow_count, 1)] = spill;
+    }
+}
+
+}  // namespace
+
+gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
+                          const uint8_t *data, const int64_t *offsets,
+                          const gbfsm_chunk_io &chunk_io, cudaStream_t stream) {
+    if (n_tasks <= 0) return GBFSM_OK;
+    ChunkIO io{chunk_io.chunks, static_cast<ChunkRecord *>(chunk_io.records),
+               chunk_io.overflow_tasks, chunk_io.overflow_count, nullptr, chunk_io.n_chunks};
+    const int warps_per_block = kLanesThreads / 32;
+    const int grid = (n_tasks + warps_per_block - 1) / warps_per_block;
+    lanes_kernel<<<grid, kLanesThreads, 0, stream>>>(table, tasks, n_tasks, data, offsets, io);
+    GBFSM_LAUNCH_CHECK("lanes_kernel launch");
+    return GBFSM_OK;
+}
+
+}  // namespace gbfsm

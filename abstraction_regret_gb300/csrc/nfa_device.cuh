@@ -533,35 +533,24 @@ struct WarpNfa {
         return finish_general(n, dense_now, info_or);
     }
 
-    // Start from the states ids[0 .. count) (distinct, already closed under epsilon).
-    __device__ GBFSM_COLD void init_ids(const uint32_t *ids, int count) {
+    // Start from the state records recs[0 .. count) (distinct states, already closed
+    // under epsilon, count <= 32), e.g. a chunk's recorded final set.
+    __device__ __forceinline__ void init_recs(const uint4 *recs, int count) {
         const uint32_t lane = lane_id();
-        if (count <= 32) {
-            mine = ((int)lane < count) ? state_record(ids[lane]) : make_uint4(0, 0, 0, 0);
-            mode = kReg;
-            m = count;
-            return;
-        }
-        // more than a register list: rebuild through V (LB when it fits, else dense)
-        uint32_t info_or = 0;
-        for (int j = (int)lane; j < count; j += 32) {
-            const uint4 rec = state_record(ids[j]);
-            if (j < S.C) S.LB[j] = rec;
-            atomicOr(reinterpret_cast<unsigned long long *>(S.V + (rec.x >> 6)),
-                     1ull << (rec.x & 63u));
-        }
-        finish_general(count, count > S.C, info_or);
+        mine = ((int)lane < count) ? recs[lane] : make_uint4(0, 0, 0, 0);
+        mode = kReg;
+        m = count;
     }
 
-    // Write the current members' ids to out[0 .. m) if there are at most `cap` of them
-    // and they are listed (REG or LIST); returns m, or -1 if not written.
-    __device__ int export_ids(uint32_t *out, int cap) const {
+    // Write the current members' records to out[0 .. m) if there are at most `cap` of
+    // them and they are listed (REG or LIST); returns m, or -1 if not written.
+    __device__ int export_recs(uint4 *out, int cap) const {
         const uint32_t lane = lane_id();
         if (m > cap || mode == kDense) return -1;
         if (mode == kReg) {
-            if ((int)lane < m) out[lane] = mine.x;
+            if ((int)lane < m) out[lane] = mine;
         } else {
-            for (int j = (int)lane; j < m; j += 32) out[j] = S.LA[j].x;
+            for (int j = (int)lane; j < m; j += 32) out[j] = S.LA[j];
         }
         return m;
     }

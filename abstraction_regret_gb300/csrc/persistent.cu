@@ -16,6 +16,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "chunks.cuh"
 #include "common.cuh"
 #include "dfa_device.cuh"
 #include "engine.hpp"
@@ -52,360 +53,6 @@ PersistLayout persist_layout(int32_t max_words, const gbfsm_plan &p) {
     L.global_per_warp = 3u * (size_t)L.wbytes;
     return L;
 }
-
-// Outcome of one chunk (GBFSM_CHUNK_RECORD_BYTES bytes). Positions are byte counts from
-// the start of the chunk's input. For a speculative chunk the set sizes are recorded
-// after 1, 2, 4, ..., 32 bytes of the chunk; acc_after[c] is the first accepting position
-// strictly after checkpoint c (-1: none before the run stopped), dead_at the position at
-// which the (superset) run died. For an input's first chunk (exact) acc_after[0] /
-// dead_at are the input's own first accept / death. end_ids lists the set at the chunk
-// end when the run got there with at most kEndCap members (end_count, else -1).
-constexpr int kCheckpoints = 6;
-constexpr int kEndCap = 32;
-struct ChunkRecord {
-    int32_t counts[kCheckpoints];
-    int32_t acc_after[kCheckpoints];
-    int32_t dead_at;
-    int32_t end_count;
-    int32_t pad[2];
-    uint32_t end_ids[kEndCap];
-};
-static_assert(sizeof(ChunkRecord) == GBFSM_CHUNK_RECORD_BYTES, "chunk record layout");
-
-__device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }
-
-// CHUNK task: run one chunk (exactly when it is the input's first) and record it.
-__device__ void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
-                          const uint8_t *base, int64_t b, int64_t e, int index,
-                          ChunkRecord *rec) {
-    const uint32_t lane = lane_id();
-    WarpNfa<false> w(nfa, R, S);
-    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
-#pragma unroll
-    for (int c = 0; c < kCheckpoints; ++c) {
-        counts[c] = 0;
-        acc_after[c] = -1;
-    }
-    int32_t dead_at = -1;
-    bool stopped = false;
-    int ev;
-    if (index == 0) {
-        ev = w.init_start();
-        if (ev == kAccept) {
-            acc_after[0] = 0;
-            stopped = true;
-        }
-    } else {
-        // superset of the true set after byte b-2, then one step on byte b-1
-        const uint32_t c0 = byte_at(base + b - 2);
-        ev = w.init_records(nfa.first_edges, __ldg(nfa.first_row + c0), __ldg(nfa.first_row + c0 + 1));
-        if (ev != kDead) ev = w.step(byte_at(base + b - 1));
-        if (ev == kDead) {
-            dead_at = (int32_t)b;
-            stopped = true;
-        }
-    }
-    const int64_t len = e - b;
-    ByteStream bytes;
-    bytes.init(base + b, stopped ? 0 : len);
-    int64_t j = 0;
-    while (!stopped && j < len) {
-        ev = w.step(bytes.next());
-        ++j;
-        const int32_t pos = (int32_t)(b + j);
-        if (index == 0) {
-            if (ev == kDead) {
-                dead_at = pos;
-                stopped = true;
-            } else if (ev == kAccept) {
-                acc_after[0] = pos;
-                stopped = true;
-            }
-            continue;
-        }
-        if (ev == kDead) {
-            dead_at = pos;
-            stopped = true;
-            break;
-        }
-        if (ev == kAccept) {
-#pragma unroll
-            for (int c = 0; c < kCheckpoints; ++c)
-                if (j > (1 << c) && acc_after[c] < 0) acc_after[c] = pos;
-            if (j > (1 << (kCheckpoints - 1))) stopped = true;  // first accept after the last checkpoint
-        }
-        if (j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) counts[31 - __clz((int)j)] = w.m;
-    }
-    int32_t end_count = -1;
-    if (!stopped) end_count = w.export_ids(rec->end_ids, kEndCap);
-    if (lane == 0) {
-#pragma unroll
-        for (int c = 0; c < kCheckpoints; ++c) {
-            rec->counts[c] = counts[c];
-            rec->acc_after[c] = acc_after[c];
-        }
-        rec->dead_at = dead_at;
-        rec->end_count = end_count;
-    }
-    w.cleanup();
-}
-
-// FIXUP task: resolve an input from its chunk records, re-running each chunk exactly only
-// until its exact set has as many members as the speculative superset at a checkpoint
-// (the superset contains the exact set, so equal sizes mean equal sets, and the rest of
-// the chunk is the recorded run).
-__device__ Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
-                             const uint8_t *base, int64_t len, const gbfsm_chunk *chunks,
-                             const ChunkRecord *recs, int first, int count, int64_t input_off) {
-    Verdict v{0, 0, len};
-    const ChunkRecord &r0 = recs[first];
-    if (r0.acc_after[0] >= 0) {
-        v.flag = 1;
-        v.len = r0.acc_after[0];
-        v.examined = r0.acc_after[0];
-        return v;
-    }
-    if (r0.dead_at >= 0) {
-        v.examined = r0.dead_at;
-        return v;
-    }
-    WarpNfa<false> w(nfa, R, S);
-    if (r0.end_count >= 0) {
-        w.init_ids(r0.end_ids, r0.end_count);
-    } else {  // the first chunk's end set was not recorded: recompute it exactly
-        w.init_start();
-        const int64_t e0 = chunks[first].end - input_off;
-        for (int64_t p = 0; p < e0; ++p) w.step(byte_at(base + p));
-    }
-    for (int k = 1; k < count; ++k) {
-        const gbfsm_chunk ch = chunks[first + k];
-        const ChunkRecord &rk = recs[first + k];
-        const int64_t b = ch.begin - input_off, e = ch.end - input_off;
-        int matched = -1;
-        int64_t j = 0;
-        while (b + j < e) {
-            const int ev = w.step(byte_at(base + b + j));
-            ++j;
-            if (ev == kDead) {
-                v.examined = b + j;
-                w.cleanup();
-                return v;
-            }
-            if (ev == kAccept) {
-                v.flag = 1;
-                v.len = (int32_t)(b + j);
-                v.examined = b + j;
-                w.cleanup();
-                return v;
-            }
-            if (matched < 0 && j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0 &&
-                w.m == rk.counts[31 - __clz((int)j)]) {
-                matched = 31 - __clz((int)j);
-                break;
-            }
-        }
-        if (matched >= 0) {
-            if (rk.acc_after[matched] >= 0) {
-                v.flag = 1;
-                v.len = rk.acc_after[matched];
-                v.examined = rk.acc_after[matched];
-                w.cleanup();
-                return v;
-            }
-            if (rk.dead_at >= 0) {
-                v.examined = rk.dead_at;
-                w.cleanup();
-                return v;
-            }
-            if (rk.end_count >= 0) {
-                w.cleanup();
-                w.init_ids(rk.end_ids, rk.end_count);
-            } else {
-                while (b + j < e) w.step(byte_at(base + b + j++));  // no event can occur here
-            }
-        }
-    }
-    w.cleanup();
-    return v;
-}
-
-// LANES task body: one chunk per lane, the set held in registers (at most kLaneCap
-// members: id and edge-row range each). Same protocol and record as run_chunk; a chunk
-// whose set outgrows the lane returns false without writing its record. The first step
-// of a speculative chunk starts from the two-byte superset pair_edges of the bytes
-// before it; each step scans a member's edge labels (edge_sym, uint16) and loads the
-// 16-byte record only of an edge that matches.
-constexpr int kLaneCap = 8;    // members a lane holds
-constexpr int kLaneMatch = 8;  // matching edges a lane handles per byte
-
-__device__ bool run_chunk_lane(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b, int64_t e,
-                               int index, ChunkRecord *rec) {
-    uint32_t ct[kLaneCap], crb[kLaneCap], cre[kLaneCap];
-    int m = 0;
-    int32_t counts[kCheckpoints], acc_after[kCheckpoints];
-#pragma unroll
-    for (int c = 0; c < kCheckpoints; ++c) {
-        counts[c] = 0;
-        acc_after[c] = -1;
-    }
-#pragma unroll
-    for (int i = 0; i < kLaneCap; ++i) ct[i] = crb[i] = cre[i] = 0;
-    int32_t dead_at = -1;
-    bool stopped = false;
-    if (index == 0) {
-        const uint32_t s = (uint32_t)A.start_state;
-        ct[0] = s;
-        crb[0] = __ldg(A.sym_row + s);
-        cre[0] = __ldg(A.sym_row + s + 1);
-        m = 1;
-        if ((__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
-             (s & 63u)) & 1ull) {
-            acc_after[0] = 0;
-            stopped = true;
-        }
-    } else {
-        const uint32_t key = (uint32_t)__ldg(base + b - 2) * 256u + (uint32_t)__ldg(base + b - 1);
-        const uint32_t pr = __ldg(A.pair_row + key), pe = __ldg(A.pair_row + key + 1);
-        if (pe - pr > (uint32_t)kLaneCap) return false;
-        m = (int)(pe - pr);
-#pragma unroll
-        for (int i = 0; i < kLaneCap; ++i) {
-            if (i < m) {
-                const uint4 r = ld_edge(A.pair_edges + pr + i);
-                ct[i] = r.x;
-                crb[i] = r.z;
-                cre[i] = r.w;
-            }
-        }
-        if (m == 0) {
-            dead_at = (int32_t)b;
-            stopped = true;
-        }
-    }
-    const int64_t len = e - b;
-    ByteStream bytes;
-    bytes.init(base + b, stopped ? 0 : len);
-    int64_t j = 0;
-    while (!stopped && j < len) {
-        const uint32_t sym = bytes.next();
-        ++j;
-        // 1. scan the members' edge labels (L1-resident uint16) for this byte, keeping the
-        //    indices of at most kLaneMatch matching edges
-        uint32_t mk[kLaneMatch];
-        int nm = 0;
-#pragma unroll
-        for (int q = 0; q < kLaneMatch; ++q) mk[q] = 0;
-#pragma unroll
-        for (int i = 0; i < kLaneCap; ++i) {
-            if (i < m) {
-                const uint32_t kb = crb[i], ke = cre[i];
-#pragma unroll 4
-                for (uint32_t k = kb; k < ke; ++k) {
-                    const uint32_t es = __ldg(A.edge_sym + k);
-                    if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) {
-#pragma unroll
-                        for (int q = 0; q < kLaneMatch; ++q)
-                            if (q == nm) mk[q] = k;
-                        ++nm;
-                    }
-                }
-            }
-        }
-        if (nm > kLaneMatch) return false;
-        // 2. load the matching edges' records together (one L2 round trip per byte)
-        uint4 rr[kLaneMatch];
-#pragma unroll
-        for (int q = 0; q < kLaneMatch; ++q)
-            rr[q] = (q < nm) ? ld_edge(A.sym_edges + mk[q]) : make_uint4(0, 0, 0, 0);
-        // 3. deduplicate the targets into the next set
-        uint32_t nt[kLaneCap], nrb[kLaneCap], nre[kLaneCap];
-        int n = 0;
-        bool acc = false, ovf = false;
-#pragma unroll
-        for (int q = 0; q < kLaneMatch; ++q) {
-            if (q < nm) {
-                const uint4 r = rr[q];
-                bool dup = false;
-#pragma unroll
-                for (int u = 0; u < q; ++u) dup |= (rr[u].x == r.x);
-                if (!dup) {
-                    if (n == kLaneCap) {
-                        ovf = true;
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < kLaneCap; ++u) {
-                            if (u == n) {
-                                nt[u] = r.x;
-                                nrb[u] = r.z;
-                                nre[u] = r.w;
-                            }
-                        }
-                        ++n;
-                        acc |= (r.y & GBFSM_EDGE_ACCEPT) != 0;
-                    }
-                }
-            }
-        }
-        if (ovf) return false;
-#pragma unroll
-        for (int q = 0; q < kLaneCap; ++q) {
-            ct[q] = nt[q];
-            crb[q] = nrb[q];
-            cre[q] = nre[q];
-        }
-        m = n;
-        const int32_t pos = (int32_t)(b + j);
-        if (index == 0) {
-            if (m == 0) {
-                dead_at = pos;
-                stopped = true;
-            } else if (acc) {
-                acc_after[0] = pos;
-                stopped = true;
-            }
-            continue;
-        }
-        if (m == 0) {
-            dead_at = pos;
-            stopped = true;
-            break;
-        }
-        if (acc) {
-#pragma unroll
-            for (int c = 0; c < kCheckpoints; ++c)
-                if (j > (1 << c) && acc_after[c] < 0) acc_after[c] = pos;
-            if (j > (1 << (kCheckpoints - 1))) stopped = true;
-        }
-        if (j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) {
-            const int c = 31 - __clz((int)j);
-#pragma unroll
-            for (int q = 0; q < kCheckpoints; ++q)
-                if (q == c) counts[q] = m;
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < kCheckpoints; ++c) {
-        rec->counts[c] = counts[c];
-        rec->acc_after[c] = acc_after[c];
-    }
-    rec->dead_at = dead_at;
-    rec->end_count = stopped ? -1 : m;
-    if (!stopped) {
-#pragma unroll
-        for (int q = 0; q < kLaneCap; ++q)
-            if (q < m) rec->end_ids[q] = ct[q];
-    }
-    return true;
-}
-
-// Device pointers of the chunk machinery, passed by value to the kernel.
-struct ChunkIO {
-    const gbfsm_chunk *chunks;
-    ChunkRecord *records;
-    gbfsm_task *overflow_tasks;
-    int32_t *overflow_count;
-    const int32_t *task_count;
-};
 
 __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persistent_kernel(
     const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
@@ -450,30 +97,12 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
             R.eps_row = nfa.eps_row;
             R.eps_edges = nfa.eps_edges;
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
-            if (task.kind == GBFSM_TASK_LANES) {
-                if ((int)lane < task.count) {
-                    const int cid = task.first + (int)lane;
-                    const gbfsm_chunk ch = chunks[cid];
-                    const int64_t off = offsets[ch.input];
-                    if (!run_chunk_lane(nfa, data + off, ch.begin - off, ch.end - off, ch.index,
-                                        records + cid)) {
-                        const int slot = atomicAdd(io.overflow_count, 1);
-                        gbfsm_task spill;
-                        spill.automaton = task.automaton;
-                        spill.first = cid;
-                        spill.count = 1;
-                        spill.kind = GBFSM_TASK_CHUNK;
-                        io.overflow_tasks[slot] = spill;
-                    }
-                }
-                __syncwarp();
-                continue;
-            }
             if (task.kind == GBFSM_TASK_CHUNK) {
                 const gbfsm_chunk ch = chunks[task.first];
                 const int64_t off = offsets[ch.input];
                 if (S.C == 0) S.C = min(L.C, 32);  // speculation keeps small sets listed
-                run_chunk(nfa, R, S, data + off, ch.begin - off, ch.end - off, ch.index,
+                run_chunk(nfa, R, S, data + off, ch.begin - off, ch.end - off,
+                          overlap_end(io, task.first, ch.end - off, off), ch.index,
                           records + task.first);
                 continue;
             }
@@ -598,13 +227,14 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
         return fail(GBFSM_INVALID_ARG, "persistent workspace too small: %zu < %zu bytes",
                     workspace_bytes, need);
     if (n_tasks <= 0) return GBFSM_OK;
-    ChunkIO io{nullptr, nullptr, nullptr, nullptr, nullptr};
+    ChunkIO io{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
     if (chunk_io) {
         io.chunks = chunk_io->chunks;
         io.records = static_cast<ChunkRecord *>(chunk_io->records);
         io.overflow_tasks = chunk_io->overflow_tasks;
         io.overflow_count = chunk_io->overflow_count;
         io.task_count = chunk_io->task_count;
+        io.n_chunks = chunk_io->n_chunks;
     }
     uint32_t *ticket = static_cast<uint32_t *>(workspace);
     uint8_t *gws = static_cast<uint8_t *>(workspace) + 256;

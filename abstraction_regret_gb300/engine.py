@@ -31,7 +31,7 @@ from __future__ import annotations
 
 import ctypes
 import time
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -69,13 +69,15 @@ class NfaChoice:
 class TaskPlan:
     """Host-side task queue of one batch."""
 
-    tasks_a: np.ndarray    # int32 [na, 4]: WHOLE and CHUNK tasks (first launch)
-    tasks_b: np.ndarray    # int32 [nb, 4]: FIXUP tasks (second launch)
+    tasks_a: np.ndarray    # int32 [na, 4]: WHOLE and CHUNK tasks (persistent launch)
+    tasks_b: np.ndarray    # int32 [nb, 4]: FIXUP tasks (last launch)
     input_ids: np.ndarray  # int32 [n]
     chunks: np.ndarray     # CHUNK_DTYPE [nc] (lane chunks first)
     chunk_bytes: int       # chunk size of warp-simulated chunks (0: none)
     lane_chunks: int = 0   # chunks run one per lane (the first lane_chunks of `chunks`)
     lane_chunk_bytes: int = 0
+    tasks_l: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int32))
+    # int32 [nl, 4]: LANES tasks (lane launch, before the persistent one)
 
 
 class DeviceTasks:
@@ -84,7 +86,7 @@ class DeviceTasks:
     def __init__(self, device) -> None:
         self.device = device
         self.cap_t = self.cap_i = self.cap_c = 0
-        self.na = self.nb = self.nc = 0
+        self.nl = self.na = self.nb = self.nc = 0
         self.n_lane_chunks = 0
 
     def chunk_io(self, overflow_count: bool = False) -> native.ChunkIO:
@@ -94,6 +96,7 @@ class DeviceTasks:
             io.records = self.d_records.data_ptr()
             io.overflow_tasks = self.d_overflow.data_ptr()
             io.overflow_count = self.d_overflow_count.data_ptr()
+            io.n_chunks = self.nc
             if overflow_count:
                 io.task_count = self.d_overflow_count.data_ptr()
         return io
@@ -118,25 +121,29 @@ class DeviceTasks:
             self.d_overflow_count = torch.zeros(4, dtype=torch.int32, device=dev)
 
     def upload(self, plan: TaskPlan, stream) -> None:
-        """Copy a plan into the pinned buffers and enqueue its host->device copies."""
-        na, nb = plan.tasks_a.shape[0], plan.tasks_b.shape[0]
+        """Copy a plan into the pinned buffers and enqueue its host->device copies. The
+        task buffer holds the LANES, persistent and FIXUP tasks back to back."""
+        nl, na, nb = plan.tasks_l.shape[0], plan.tasks_a.shape[0], plan.tasks_b.shape[0]
         nc = plan.chunks.shape[0]
-        self._ensure(na + nb + 1, plan.input_ids.size + 1, nc + 1)
+        self._ensure(nl + na + nb + 1, plan.input_ids.size + 1, nc + 1)
+        h = self.h_tasks.numpy()
+        if nl:
+            h[: nl * 4] = plan.tasks_l.reshape(-1)
         if na:
-            self.h_tasks.numpy()[: na * 4] = plan.tasks_a.reshape(-1)
+            h[nl * 4:(nl + na) * 4] = plan.tasks_a.reshape(-1)
         if nb:
-            self.h_tasks.numpy()[na * 4:(na + nb) * 4] = plan.tasks_b.reshape(-1)
+            h[(nl + na) * 4:(nl + na + nb) * 4] = plan.tasks_b.reshape(-1)
         self.h_ids.numpy()[: plan.input_ids.size] = plan.input_ids
         if nc:
             self.h_chunks.numpy()[: nc * 24] = plan.chunks.view(np.uint8)
         with torch.cuda.stream(stream):
-            nt = max(1, na + nb) * 4
+            nt = max(1, nl + na + nb) * 4
             self.d_tasks[:nt].copy_(self.h_tasks[:nt], non_blocking=True)
             ni = max(1, plan.input_ids.size)
             self.d_ids[:ni].copy_(self.h_ids[:ni], non_blocking=True)
             if nc:
                 self.d_chunks[: nc * 24].copy_(self.h_chunks[: nc * 24], non_blocking=True)
-        self.na, self.nb, self.nc = na, nb, nc
+        self.nl, self.na, self.nb, self.nc = nl, na, nb, nc
         self.n_lane_chunks = int(plan.lane_chunks)
 
 
@@ -267,14 +274,16 @@ class PersistentEngine:
                 chunk_l = self.auto_chunk_bytes(int(lengths[lane_in].sum()), LANE_GROUP)
             csize[warp_in] = chunk_w
             csize[lane_in] = chunk_l
-        split = (csize > 0) & (lengths >= 2 * np.maximum(csize, 1))
+        # every input of a lane automaton is chunked (a short one is a single exact
+        # chunk); warp-chunked inputs are split when they span two chunks or more
+        split = (csize > 0) & ((lengths >= 2 * np.maximum(csize, 1)) | lane_in)
         whole = nfa_idx[~split[nfa_idx]]
         pos_of = np.empty(n, dtype=np.int64)
         pos_of[nfa_idx] = np.arange(nfa_idx.size)
         rows.append(np.stack([aut_ids[whole], pos_of[whole], np.ones_like(whole),
                               np.full_like(whole, native.TASK_WHOLE),
                               lengths[whole] * NFA_BYTE_WEIGHT], axis=1))
-        chunk_list, fix_rows = [], []
+        chunk_list, fix_rows, lane_rows = [], [], []
         n_lane = 0
         if split.any():
             # lane-chunked inputs first (grouped by automaton), then warp-chunked ones
@@ -283,19 +292,20 @@ class PersistentEngine:
             sw = np.flatnonzero(split & ~lane_in)
             sidx = np.concatenate([sl, sw])
             cs = csize[sidx]
-            counts = lengths[sidx] // cs  # the last chunk absorbs the remainder
+            # ceil(length / size) chunks of even length (each in (size/2, size])
+            counts = np.maximum(1, -(-lengths[sidx] // cs))
             first = np.zeros(sidx.size, dtype=np.int64)
             np.cumsum(counts[:-1], out=first[1:])
             total = int(counts.sum())
             ch = np.zeros(total, dtype=native.CHUNK_DTYPE)
             inp = np.repeat(sidx, counts)
             idx = np.arange(total) - np.repeat(first, counts)
-            csz = np.repeat(cs, counts)
+            cnt = np.repeat(counts, counts)
+            ln = lengths[inp]
             ch["input"] = inp
             ch["index"] = idx
-            ch["begin"] = starts[inp] + idx * csz
-            last = idx == np.repeat(counts - 1, counts)
-            ch["end"] = np.where(last, starts[inp] + lengths[inp], ch["begin"] + csz)
+            ch["begin"] = starts[inp] + idx * ln // cnt
+            ch["end"] = starts[inp] + (idx + 1) * ln // cnt
             n_lane = int(counts[:sl.size].sum())
             if n_lane and data is not None:
                 self._shift_boundaries(ch[:n_lane], inp[:n_lane], aut_ids[inp[:n_lane]],
@@ -314,9 +324,8 @@ class PersistentEngine:
                         gc.append(min(LANE_GROUP, e0 - g))
                 g0 = np.asarray(g0, dtype=np.int64)
                 gc = np.asarray(gc, dtype=np.int64)
-                gmax = np.maximum.reduceat(clen[:n_lane], g0)
-                rows.append(np.stack([la[g0], g0, gc, np.full(g0.size, native.TASK_LANES),
-                                      gmax * NFA_BYTE_WEIGHT], axis=1))
+                lane_rows.append(np.stack([la[g0], g0, gc, np.full(g0.size, native.TASK_LANES)],
+                                          axis=1))
             wc = np.arange(n_lane, total)
             if wc.size:
                 rows.append(np.stack([aut_ids[inp[wc]], wc, np.ones(wc.size, np.int64),
@@ -338,6 +347,7 @@ class PersistentEngine:
                                   np.full(g.size, native.TASK_WHOLE), lengths[dfa_idx[g]]], axis=1))
         t = np.concatenate(rows)
         t = t[np.argsort(-t[:, 4], kind="stable")][:, :4]
+        lanes = np.concatenate(lane_rows) if lane_rows else empty
         if fix_rows:
             f = np.concatenate(fix_rows)
             f = f[np.argsort(-f[:, 4], kind="stable")][:, :4]
@@ -346,7 +356,7 @@ class PersistentEngine:
         chunks = np.concatenate(chunk_list) if chunk_list else no_chunks
         return TaskPlan(np.ascontiguousarray(t, dtype=np.int32),
                         np.ascontiguousarray(f, dtype=np.int32), input_ids, chunks, chunk_w,
-                        n_lane, chunk_l)
+                        n_lane, chunk_l, np.ascontiguousarray(lanes, dtype=np.int32))
 
     # ---- launches -------------------------------------------------------------------------
 
@@ -369,27 +379,37 @@ class PersistentEngine:
 
     def launch(self, d_data, d_off, dt: DeviceTasks, d_flags, d_lens, d_examined=None,
                stream=None, d_ends=None, workspace=None) -> int:
-        """Enqueue the batch's launches (one, or two with speculative chunks); returns how
-        many kernels were launched. ``d_data`` is a device tensor or a raw device address
-        (e.g. of pinned host memory read in place); with ``d_ends`` input i spans
-        ``[d_off[i], d_ends[i])``."""
+        """Enqueue the batch's launches; returns how many kernels were launched:
+        the lane launch (LANES tasks), the persistent launch (WHOLE / CHUNK tasks), the
+        overflow pass (lane chunks that outgrew their lane, run by warps) and the fix-up
+        (FIXUP tasks), each only when it has work. ``d_data`` is a device tensor or a raw
+        device address (e.g. of pinned host memory read in place); with ``d_ends`` input
+        i spans ``[d_off[i], d_ends[i])``."""
         stream = stream or torch.cuda.current_stream(self.device)
         ws = self.workspace if workspace is None else workspace
         data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
         base = dt.d_tasks.data_ptr()
-        launches = 1
-        if dt.n_lane_chunks:
+        launches = 0
+        if dt.nl:
             with torch.cuda.stream(stream):
                 dt.d_overflow_count.zero_()
-        self._run(base, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens, d_examined, ws,
-                  stream)
-        if dt.n_lane_chunks:  # chunks that outgrew their lane, run by warps
+            io = dt.chunk_io()
+            st = native.lib().gbfsm_lanes_run(
+                self.table.data_ptr(), len(self.automata), base, dt.nl, data_ptr,
+                d_off.data_ptr(), ctypes.byref(io), stream.cuda_stream)
+            native.check(st, "gbfsm_lanes_run")
+            launches += 1
+        if dt.na or not (dt.nl or dt.nb):
+            self._run(base + dt.nl * 16, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
+                      d_examined, ws, stream)
+            launches += 1
+        if dt.nl:
             self._run(dt.d_overflow.data_ptr(), dt.n_lane_chunks, dt, data_ptr, d_off, d_ends,
                       d_flags, d_lens, d_examined, ws, stream, overflow_pass=True)
             launches += 1
         if dt.nb:
-            self._run(base + dt.na * 16, dt.nb, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
-                      d_examined, ws, stream)
+            self._run(base + (dt.nl + dt.na) * 16, dt.nb, dt, data_ptr, d_off, d_ends, d_flags,
+                      d_lens, d_examined, ws, stream)
             launches += 1
         return launches
 
@@ -465,7 +485,8 @@ class GraphRunner:
         self.with_examined = with_examined
         self.stream = torch.cuda.Stream(dev)
         p = self.task_plan
-        self.h2d_bytes = padded + self.h_off.numel() * 8 + (p.tasks_a.shape[0] +
+        self.h2d_bytes = padded + self.h_off.numel() * 8 + (p.tasks_l.shape[0] +
+                                                             p.tasks_a.shape[0] +
                                                              p.tasks_b.shape[0]) * 16 + \
             p.input_ids.size * 4 + p.chunks.shape[0] * 24
         self.d2h_bytes = self.h_out.numel() * 4

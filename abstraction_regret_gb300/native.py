@@ -108,12 +108,12 @@ class Chunk(ctypes.Structure):
 class ChunkIO(ctypes.Structure):
     _fields_ = [("chunks", ctypes.c_void_p), ("records", ctypes.c_void_p),
                 ("overflow_tasks", ctypes.c_void_p), ("overflow_count", ctypes.c_void_p),
-                ("task_count", ctypes.c_void_p)]
+                ("task_count", ctypes.c_void_p), ("n_chunks", ctypes.c_int32)]
 
 
 TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES = 0, 1, 2, 3
-LANE_CAPACITY = 8  # members a lane holds (kLaneCap)
-CHUNK_RECORD_BYTES = 192
+LANE_CAPACITY = 4  # members a lane holds (kLaneSlots)
+CHUNK_RECORD_BYTES = 256
 CHUNK_DTYPE = [("input", "<i4"), ("index", "<i4"), ("begin", "<i8"), ("end", "<i8")]
 
 
@@ -155,6 +155,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_run_dfa_bytes": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                            _vp]),
     "gbfsm_host_device_pointer": (ctypes.c_int, [_vp, _P(_vp)]),
+    "gbfsm_lanes_run": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _P(ChunkIO), _vp]),
     "gbfsm_workload_walk": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _u64, _vp, _i32]),
 }
 

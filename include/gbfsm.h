@@ -243,7 +243,7 @@ typedef struct gbfsm_chunk {
 } gbfsm_chunk;
 
 /* Bytes of one chunk record (device scratch written by CHUNK tasks, read by FIXUP). */
-#define GBFSM_CHUNK_RECORD_BYTES 192
+#define GBFSM_CHUNK_RECORD_BYTES 256
 
 /* Device buffers of the speculative-chunk machinery (all device pointers; passed by
  * host pointer, NULL when a launch has no CHUNK, LANES or FIXUP task). */
@@ -255,6 +255,7 @@ typedef struct gbfsm_chunk_io {
                                      the launch that runs LANES tasks */
     const int32_t *task_count;    /* non-NULL: run min(*task_count, n_tasks) tasks, a count
                                      written on the device by an earlier launch */
+    int32_t n_chunks;             /* entries of the chunk table */
 } gbfsm_chunk_io;
 
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
@@ -282,6 +283,15 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
  * read request bytes in place over the host link instead of copying them first. No
  * counterpart in the reference (which copies every input, common.cuh:150-159). */
 gbfsm_status gbfsm_host_device_pointer(void *host, void **device);
+
+/* Run LANES tasks (one warp per task, one chunk per lane), writing chunk records and
+ * appending chunks that outgrow a lane to chunk_io->overflow_tasks (the caller zeroes
+ * overflow_count first). data/offsets as for gbfsm_persistent_run (contiguous inputs:
+ * input i starts at offsets[i]). No counterpart in the reference. */
+gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
+                             const gbfsm_task *tasks, int32_t n_tasks, const uint8_t *data,
+                             const int64_t *offsets, const gbfsm_chunk_io *chunk_io,
+                             void *stream);
 
 /* Occupancy query for persistent launches: CTAs of `plan` resident per SM. */
 int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan);

@@ -9,6 +9,13 @@ chunk exactly until the exact set is as large as the superset at a checkpoint. T
 model must give the oracle's verdict on every input, for any chunk size -- this pins the
 protocol itself, independently of the kernels (the GPU tests pin the kernels against
 the oracle).
+
+``scan_fixup`` restates the parallel form of the fix-up (csrc/chunks.cuh): each chunk
+also continues its run up to 32 bytes into the next chunk (the overlap), and a chunk is
+linked to its predecessor when the overlap run has the next chunk's recorded size at a
+checkpoint. A chain of links from the exact first chunk makes every linked chunk's
+record exact, so the fix-up is a scan for the first chunk that decides (an accept or a
+death) or cannot be linked; only from there does it fall back to the serial re-run.
 """
 
 from __future__ import annotations
@@ -40,9 +47,11 @@ def accepts(nfa, cur):
     return any(nfa.accept[s] for s in cur)
 
 
-def run_chunk(nfa, data, b, e, index, lists):
+def run_chunk(nfa, data, b, e, index, lists, ov_end=None):
     rec = {"counts": [0] * CHECKPOINTS, "acc_after": [-1] * CHECKPOINTS, "dead_at": -1,
-           "end": None}
+           "end": None, "ov_len": 0, "ov_counts": [0] * CHECKPOINTS, "ov_acc": 0,
+           "ov_dead": 0}
+    ov_end = e if ov_end is None else ov_end
     if index == 0:
         cur = epsilon_closure({int(nfa.start_state)}, nfa)
         if accepts(nfa, cur):
@@ -79,17 +88,30 @@ def run_chunk(nfa, data, b, e, index, lists):
         if j <= (1 << (CHECKPOINTS - 1)) and (j & (j - 1)) == 0:
             rec["counts"][j.bit_length() - 1] = len(cur)
     rec["end"] = set(cur)
+    if ov_end > e:  # the overlap: continue into the next chunk from the end set
+        rec["ov_len"] = ov_end - e
+        for j in range(1, ov_end - e + 1):
+            cur = step(nfa, cur, data[e + j - 1])
+            if not cur:
+                rec["ov_dead"] = j
+                break
+            if accepts(nfa, cur):
+                rec["ov_acc"] = j
+                break
+            if j <= 32 and (j & (j - 1)) == 0:
+                rec["ov_counts"][j.bit_length() - 1] = len(cur)
     return rec
 
 
-def run_fixup(nfa, data, chunks, recs):
+def run_fixup(nfa, data, chunks, recs, start=1):
+    """Serial fix-up from chunk ``start`` (>= 1), whose predecessor's end set is exact."""
     r0 = recs[0]
     if r0["acc_after"][0] >= 0:
         return True, r0["acc_after"][0]
     if r0["dead_at"] >= 0:
         return False, 0
-    cur = r0["end"]
-    for (b, e), rk in zip(chunks[1:], recs[1:]):
+    cur = recs[start - 1]["end"]
+    for (b, e), rk in zip(chunks[start:], recs[start:]):
         matched = -1
         j = 0
         while b + j < e:
@@ -116,14 +138,70 @@ def run_fixup(nfa, data, chunks, recs):
     return False, 0
 
 
-def speculative(nfa, data: bytes, chunk: int):
+LINK, DECIDE, BREAK = 0, 1, 2
+
+
+def classify(prev, rk, begin):
+    """Chunk k against its predecessor's overlap run: LINK (exact from a checkpoint on,
+    no event), DECIDE with the verdict, or BREAK (no link within the overlap)."""
+    for c in range(CHECKPOINTS):
+        j = 1 << c
+        if j > prev["ov_len"]:
+            break
+        if prev["ov_acc"] and prev["ov_acc"] <= j:
+            return DECIDE, (True, begin + prev["ov_acc"])
+        if prev["ov_dead"] and prev["ov_dead"] <= j:
+            return DECIDE, (False, 0)
+        if prev["ov_counts"][c] == rk["counts"][c]:
+            if rk["acc_after"][c] >= 0:
+                return DECIDE, (True, rk["acc_after"][c])
+            if rk["dead_at"] >= 0:
+                return DECIDE, (False, 0)
+            return LINK, None
+    return BREAK, None
+
+
+def scan_fixup(nfa, data, chunks, recs):
+    r0 = recs[0]
+    if r0["acc_after"][0] >= 0:
+        return True, r0["acc_after"][0]
+    if r0["dead_at"] >= 0:
+        return False, 0
+    last_rec = 0 if r0["end"] is not None else -1
+    for k in range(1, len(chunks)):
+        status, verdict = classify(recs[k - 1], recs[k], chunks[k][0])
+        if status == DECIDE:
+            return verdict
+        if status == BREAK:
+            if last_rec < 0:
+                return simulate(nfa, data)
+            return run_fixup(nfa, data, chunks, recs, start=last_rec + 1)
+        if recs[k]["end"] is not None:
+            last_rec = k
+    return False, 0
+
+
+def even_bounds(n: int, chunk: int):
+    count = max(1, -(-n // chunk))
+    return [(k * n // count, (k + 1) * n // count) for k in range(count)]
+
+
+def speculative(nfa, data: bytes, chunk: int, scan: bool = False, even: bool = False):
     n = len(data)
-    if n < 2 * chunk:
+    if n < 2 * chunk and not even:
         return simulate(nfa, data)
     lists = first_lists(nfa)
-    count = n // chunk
-    bounds = [(k * chunk, (k + 1) * chunk if k < count - 1 else n) for k in range(count)]
-    recs = [run_chunk(nfa, data, b, e, k, lists) for k, (b, e) in enumerate(bounds)]
+    if even:
+        bounds = even_bounds(n, chunk)
+    else:
+        count = n // chunk
+        bounds = [(k * chunk, (k + 1) * chunk if k < count - 1 else n) for k in range(count)]
+    recs = []
+    for k, (b, e) in enumerate(bounds):
+        ov_end = min(e + 32, bounds[k + 1][1]) if k + 1 < len(bounds) else e
+        recs.append(run_chunk(nfa, data, b, e, k, lists, ov_end))
+    if scan:
+        return scan_fixup(nfa, data, bounds, recs)
     return run_fixup(nfa, data, bounds, recs)
 
 
@@ -148,8 +226,14 @@ def test_protocol_matches_the_oracle_on_fuzz(seed):
         nfa = _fuzz_nfa(rng, rng.randint(1, 40), "abc", 0.03, 0.05, rng.choice([0, 1, 2]))
         for _ in range(4):
             data = bytes(ord(rng.choice("abc")) for _ in range(rng.randint(0, 400)))
+            want = simulate(nfa, data)
             for chunk in (40, 64, 97):
-                assert speculative(nfa, data, chunk) == simulate(nfa, data)
+                assert speculative(nfa, data, chunk) == want
+                assert speculative(nfa, data, chunk, scan=True) == want
+            for chunk in (9, 17):  # overlaps shorter than 32 bytes
+                assert speculative(nfa, data, chunk, scan=True) == want
+            if len(data) >= 64:
+                assert speculative(nfa, data, 64, scan=True, even=True) == want
 
 
 def test_protocol_on_live_walks_of_the_large_configuration():
@@ -158,5 +242,7 @@ def test_protocol_on_live_walks_of_the_large_configuration():
     idx = np.argsort(np.diff(b.offsets))[:12]
     for i in idx:
         data = b.inputs([int(i)])[0][:6000]
+        want = simulate(nfa, data)
         for chunk in (256, 1000):
-            assert speculative(nfa, data, chunk) == simulate(nfa, data)
+            assert speculative(nfa, data, chunk) == want
+            assert speculative(nfa, data, chunk, scan=True, even=True) == want
