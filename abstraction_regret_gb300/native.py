@@ -114,6 +114,7 @@ class ChunkIO(ctypes.Structure):
 TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES = 0, 1, 2, 3
 LANE_CAPACITY = 4  # members a lane holds (kLaneSlots)
 CHUNK_RECORD_BYTES = 256
+STATIC_SCRATCH_BYTES = 32 << 20  # GBFSM_STATIC_SCRATCH_BYTES
 CHUNK_DTYPE = [("input", "<i4"), ("index", "<i4"), ("begin", "<i8"), ("end", "<i8")]
 
 
@@ -156,6 +157,8 @@ SIGNATURES: dict[str, tuple] = {
                                            _vp]),
     "gbfsm_host_device_pointer": (ctypes.c_int, [_vp, _P(_vp)]),
     "gbfsm_lanes_run": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _P(ChunkIO), _vp]),
+    "gbfsm_nfa_run_static": (ctypes.c_int, [_P(NfaDev), _vp, _vp, _i32, _P(Plan), _vp, _vp,
+                                            _vp, _vp]),
     "gbfsm_workload_walk": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _u64, _vp, _i32]),
 }
 

@@ -187,6 +187,26 @@ gbfsm_status gbfsm_nfa_run(const gbfsm_nfa_dev *nfa, const uint8_t *data,
                            int32_t *flags, int32_t *lens, int32_t *examined, void *workspace,
                            size_t workspace_bytes, void *stream);
 
+/* Size of the fixed device scratch of gbfsm_nfa_run_static (32 MiB per device). */
+#define GBFSM_STATIC_SCRATCH_BYTES (32u << 20)
+
+/* gbfsm_nfa_run without a workspace argument: the scratch comes from a fixed array of
+ * GBFSM_STATIC_SCRATCH_BYTES in device memory, so the call allocates nothing on the
+ * device (no cudaMalloc / cudaFree, no allocator of any library). For callers that
+ * cannot allocate device memory themselves, e.g. a foreign-language host without a
+ * device allocator, or a service that must not grow its device footprint or wait on
+ * an allocator while requests are in flight. Returns GBFSM_INVALID_ARG, writing
+ * nothing, when the batch needs more scratch than that (gbfsm_nfa_workspace_bytes of
+ * the same arguments). The first call on a device looks up the array's address
+ * (module load); make it before any stream capture. All calls on a device share the
+ * one array: calls whose kernels overlap on the GPU race on it and must be ordered
+ * (e.g. issued on one stream). Results are those of gbfsm_nfa_run. No counterpart in
+ * the reference. */
+gbfsm_status gbfsm_nfa_run_static(const gbfsm_nfa_dev *nfa, const uint8_t *data,
+                                  const int64_t *offsets, int32_t n_inputs,
+                                  const gbfsm_plan *plan, int32_t *flags, int32_t *lens,
+                                  int32_t *examined, void *stream);
+
 /* Simulate `dfa` over a batch (thread per input; table in shared memory when
  * plan->stage and it fits, else read through L2). */
 gbfsm_status gbfsm_dfa_run(const gbfsm_dfa_dev *dfa, const uint8_t *data,

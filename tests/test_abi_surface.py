@@ -65,12 +65,13 @@ def test_struct_layouts_match_the_header(tmp_path):
     pairs = {"gbfsm_edge": native.Edge, "gbfsm_nfa_dev": native.NfaDev,
              "gbfsm_dfa_dev": native.DfaDev, "gbfsm_plan": native.Plan,
              "gbfsm_automaton": native.Automaton, "gbfsm_task": native.Task,
-             "gbfsm_chunk": native.Chunk}
+             "gbfsm_chunk": native.Chunk, "gbfsm_chunk_io": native.ChunkIO}
     src = tmp_path / "probe.c"
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gbfsm.h"', "int main(void) {"]
     for name in pairs:
         lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
     lines.append('  printf("record %d\\n", GBFSM_CHUNK_RECORD_BYTES);')
+    lines.append('  printf("static %u\\n", GBFSM_STATIC_SCRATCH_BYTES);')
     lines.append("  return 0; }")
     src.write_text("\n".join(lines))
     exe = tmp_path / "probe"
@@ -80,6 +81,7 @@ def test_struct_layouts_match_the_header(tmp_path):
     for name, cls in pairs.items():
         assert int(out[name]) == ctypes.sizeof(cls), name
     assert int(out["record"]) == native.CHUNK_RECORD_BYTES
+    assert int(out["static"]) == native.STATIC_SCRATCH_BYTES
     assert np.dtype(native.CHUNK_DTYPE).itemsize == ctypes.sizeof(native.Chunk)
 
 
