@@ -41,7 +41,8 @@ constexpr int kLaneSlots = 4;    // states (and matching edges per byte) a lane 
 // records, when the run got there with at most kEndCap members (end_count, else -1).
 // The overlap run (from the end set into the next chunk of the same input): ov_len bytes
 // stepped, ov_event = +j / -j when it accepted / died at its j-th byte (0: neither),
-// ov_counts[c] its size after 2^c bytes.
+// ov_counts[c] its size after 2^c bytes. begin / end: the bounds the chunk actually ran
+// over (chunk_bounds), input-relative.
 struct ChunkRecord {
     int32_t counts[kCheckpoints];
     int32_t acc_after[kCheckpoints];
@@ -50,7 +51,9 @@ struct ChunkRecord {
     int32_t ov_len;
     int32_t ov_event;
     int32_t ov_counts[kCheckpoints];
-    int32_t pad[10];
+    int64_t begin;
+    int64_t end;
+    int32_t pad[6];
     uint4 end_recs[kEndCap];
 };
 static_assert(sizeof(ChunkRecord) == GBFSM_CHUNK_RECORD_BYTES, "chunk record layout");
@@ -65,17 +68,67 @@ struct ChunkIO {
     int32_t n_chunks;
 };
 
-// End (input-relative, like b and e) of the overlap run of chunk `cid` ending at e: up to
-// kOverlap bytes into the next chunk when that chunk belongs to the same input.
-__device__ __forceinline__ int64_t overlap_end(const ChunkIO &io, int cid, int64_t e,
-                                               int64_t off) {
-    if (cid + 1 >= io.n_chunks) return e;
-    const gbfsm_chunk nx = io.chunks[cid + 1];
-    if (nx.index == 0) return e;
-    return min(e + (int64_t)kOverlap, nx.end - off);
+__device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }
+
+constexpr int kShiftWindow = 32;    // bytes a chunk start may move forward
+constexpr uint32_t kShiftSet = 4u;  // a two-byte superset this small ends the search
+
+// Start of a later chunk whose nominal bounds are [nb, ne) (input-relative). For an
+// automaton with a two-byte superset table the start moves forward to the first position
+// of its first min(kShiftWindow, (ne - nb) / 4) bytes whose superset has at most kShiftSet
+// states (the smallest superset when none does): a smaller starting superset converges
+// sooner and rarely outgrows a lane. The rule is a pure function of the chunk table and
+// the bytes, so the chunk and its predecessor (whose end it is) agree without exchange.
+__device__ __forceinline__ int64_t chunk_start(const gbfsm_nfa_dev &A, const uint8_t *base,
+                                               int64_t nb, int64_t ne) {
+    if (A.pair_row == nullptr) return nb;
+    const int w = (int)min((int64_t)kShiftWindow, max((int64_t)1, (ne - nb) / 4));
+    uint32_t prev = byte_at(base + nb - 2), cur = byte_at(base + nb - 1);
+    int best = 0;
+    uint32_t best_size = 0xffffffffu;
+    for (int t = 0; t < w; ++t) {
+        const uint32_t key = prev * 256u + cur;
+        const uint32_t size = __ldg(A.pair_row + key + 1) - __ldg(A.pair_row + key);
+        if (size <= kShiftSet) {
+            best = t;
+            break;
+        }
+        if (size < best_size) {
+            best_size = size;
+            best = t;
+        }
+        prev = cur;
+        cur = byte_at(base + nb + t);
+    }
+    return nb + best;
 }
 
-__device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }
+// Bounds a chunk runs over (input-relative): its start (moved by chunk_start unless it
+// is the input's first chunk), its end (the next chunk's start, or the input end), and
+// the end of its overlap run: up to kOverlap bytes into the next chunk, never past that
+// chunk's nominal end (which its actual end cannot precede).
+struct Bounds {
+    int64_t b, e, ov_end;
+};
+
+__device__ __forceinline__ Bounds chunk_bounds(const ChunkIO &io, const gbfsm_nfa_dev &A,
+                                               const uint8_t *base, int cid, int64_t off) {
+    const gbfsm_chunk ch = io.chunks[cid];
+    Bounds r;
+    r.b = ch.begin - off;
+    r.e = ch.end - off;
+    if (ch.index > 0) r.b = chunk_start(A, base, r.b, r.e);
+    r.ov_end = r.e;
+    if (cid + 1 < io.n_chunks) {
+        const gbfsm_chunk nx = io.chunks[cid + 1];
+        if (nx.index != 0) {
+            const int64_t nb = nx.begin - off, ne = nx.end - off;
+            r.e = chunk_start(A, base, nb, ne);
+            r.ov_end = min(r.e + (int64_t)kOverlap, ne);
+        }
+    }
+    return r;
+}
 
 __device__ __forceinline__ int checkpoint_of(int64_t j) {
     return (j >= 1 && j <= (1 << (kCheckpoints - 1)) && (j & (j - 1)) == 0) ? 31 - __clz((int)j)
@@ -185,6 +238,8 @@ __device__ inline void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpSc
         }
         rec->dead_at = dead_at;
         rec->end_count = end_count;
+        rec->begin = b;
+        rec->end = e;
         write_overlap(rec, ov_len, ov_event, ov_counts);
     }
     w.cleanup();
@@ -324,6 +379,8 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
     }
     rec->dead_at = dead_at;
     rec->end_count = stopped ? -1 : m;
+    rec->begin = b;
+    rec->end = e;
     int32_t ov_len = 0, ov_event = 0, ov_counts[kCheckpoints];
 #pragma unroll
     for (int c = 0; c < kCheckpoints; ++c) ov_counts[c] = 0;
@@ -370,8 +427,7 @@ struct RecordHead {
     int64_t end;
 };
 
-__device__ __forceinline__ RecordHead load_head(const gbfsm_chunk *chunks,
-                                                const ChunkRecord *recs, int k) {
+__device__ __forceinline__ RecordHead load_head(const ChunkRecord *recs, int k) {
     RecordHead h;
     const ChunkRecord &r = recs[k];
 #pragma unroll
@@ -381,8 +437,8 @@ __device__ __forceinline__ RecordHead load_head(const gbfsm_chunk *chunks,
     }
     h.dead_at = r.dead_at;
     h.end_count = r.end_count;
-    h.begin = chunks[k].begin;
-    h.end = chunks[k].end;
+    h.begin = r.begin;
+    h.end = r.end;
     return h;
 }
 
@@ -432,14 +488,14 @@ __device__ __forceinline__ Verdict decided(int32_t flag, int64_t pos) {
 // Serial re-run of chunks [start, count) from the exact set already in `w`; the part of
 // the fix-up that runs only from a chunk the scan could not link.
 __device__ inline Verdict serial_fixup(WarpNfa<false> &w, const uint8_t *base, int64_t len,
-                                       const gbfsm_chunk *chunks, const ChunkRecord *recs,
-                                       int first, int start, int count, int64_t input_off) {
+                                       const ChunkRecord *recs, int first, int start,
+                                       int count) {
     Verdict v{0, 0, len};
-    RecordHead next = load_head(chunks, recs, first + start);
+    RecordHead next = load_head(recs, first + start);
     for (int k = start; k < count; ++k) {
         const RecordHead rk = next;
-        if (k + 1 < count) next = load_head(chunks, recs, first + k + 1);  // prefetch
-        const int64_t b = rk.begin - input_off, e = rk.end - input_off;
+        if (k + 1 < count) next = load_head(recs, first + k + 1);  // prefetch
+        const int64_t b = rk.begin, e = rk.end;
         int matched = -1;
         int64_t j = 0;
         while (b + j < e) {
@@ -468,9 +524,8 @@ __device__ inline Verdict serial_fixup(WarpNfa<false> &w, const uint8_t *base, i
 }
 
 __device__ inline Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, WarpScratch S,
-                                    const uint8_t *base, int64_t len, const gbfsm_chunk *chunks,
-                                    const ChunkRecord *recs, int first, int count,
-                                    int64_t input_off) {
+                                    const uint8_t *base, int64_t len, const ChunkRecord *recs,
+                                    int first, int count) {
     const uint32_t lane = lane_id();
     const ChunkRecord &r0 = recs[first];
     if (r0.acc_after[0] >= 0) return decided(1, r0.acc_after[0]);
@@ -486,8 +541,7 @@ __device__ inline Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, War
         bool rec_ok = false;
         if (k < count) {
             const ChunkRecord &rk = recs[first + k];
-            status = classify(recs[first + k - 1], rk, chunks[first + k].begin - input_off,
-                              flag, pos);
+            status = classify(recs[first + k - 1], rk, rk.begin, flag, pos);
             rec_ok = rk.end_count >= 0;
         }
         const uint32_t stop = __ballot_sync(GBFSM_FULL_MASK, status != kLink);
@@ -512,11 +566,11 @@ __device__ inline Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, War
         start = last_rec + 1;
     } else {  // the first chunk's final set was not recorded: recompute it exactly
         w.init_start();
-        const int64_t e0 = chunks[first].end - input_off;
+        const int64_t e0 = recs[first].end;
         for (int64_t p = 0; p < e0; ++p) w.step(byte_at(base + p));
         start = 1;
     }
-    const Verdict v = serial_fixup(w, base, len, chunks, recs, first, start, count, input_off);
+    const Verdict v = serial_fixup(w, base, len, recs, first, start, count);
     w.cleanup();
     return v;
 }

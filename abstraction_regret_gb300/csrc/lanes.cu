@@ -33,9 +33,8 @@ __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
     const gbfsm_chunk ch = io.chunks[cid];
     const int64_t off = offsets[ch.input];
     const gbfsm_nfa_dev &A = table[task.automaton].nfa;
-    const int64_t e = ch.end - off;
-    if (!lane_chunk(A, data + off, ch.begin - off, e, overlap_end(io, cid, e, off), ch.index,
-                    io.records + cid)) {
+    const Bounds bd = chunk_bounds(io, A, data + off, cid, off);
+    if (!lane_chunk(A, data + off, bd.b, bd.e, bd.ov_end, ch.index, io.records + cid)) {
         gbfsm_task spill;
         spill.automaton = task.automaton;
         spill.first = cid;

@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
                 const gbfsm_chunk ch = chunks[task.first];
                 const int64_t off = offsets[ch.input];
                 if (S.C == 0) S.C = min(L.C, 32);  // speculation keeps small sets listed
-                run_chunk(nfa, R, S, data + off, ch.begin - off, ch.end - off,
-                          overlap_end(io, task.first, ch.end - off, off), ch.index,
+                const Bounds bd = chunk_bounds(io, nfa, data + off, task.first, off);
+                run_chunk(nfa, R, S, data + off, bd.b, bd.e, bd.ov_end, ch.index,
                           records + task.first);
                 continue;
             }
@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
                 const int64_t off = offsets[id];
                 const int64_t e = ends ? ends[id] : offsets[id + 1];
                 if (S.C == 0) S.C = min(L.C, 32);
-                const Verdict v = run_fixup(nfa, R, S, data + off, e - off, chunks, records,
-                                            task.first, task.count, off);
+                const Verdict v = run_fixup(nfa, R, S, data + off, e - off, records,
+                                            task.first, task.count);
                 if (lane == 0) {
                     flags[id] = v.flag;
                     lens[id] = v.len;

@@ -49,10 +49,8 @@ LANE_GROUP = 32      # chunks per LANES task (one per lane)
 # an automaton's chunks run one per lane when its two-byte supersets are this small on
 # average (the lane holds at most native.LANE_CAPACITY states; larger sets spill to warps)
 LANE_PAIR_MEAN = 4.0
-# a lane chunk's start is moved forward (by less than BOUNDARY_WINDOW bytes) to the first
-# position whose two-byte superset has at most BOUNDARY_SET states, when one exists
-BOUNDARY_WINDOW = 32
-BOUNDARY_SET = 4
+# resident warps per SM of the lane launch (128-thread CTAs, 8 per SM: csrc/lanes.cu)
+LANE_WARPS_PER_SM = 32
 
 
 @dataclass
@@ -200,47 +198,36 @@ class PersistentEngine:
             raw = np.frombuffer(bytes(table), dtype=np.uint8).copy()
             self.table = torch.from_numpy(raw).to(self.device)
             props = torch.cuda.get_device_properties(self.device)
-        self.resident_warps = props.multi_processor_count * self.ctas_per_sm * (block_threads // 32)
+        self.sm_count = props.multi_processor_count
+        self.resident_warps = self.sm_count * self.ctas_per_sm * (block_threads // 32)
         self._staging = Staging(self.device)
         self._results = Results(self.device)
         self._tasks = DeviceTasks(self.device)
 
     # ---- task queue ---------------------------------------------------------------------
 
-    def auto_chunk_bytes(self, nfa_bytes: int, per_warp: int = 1) -> int:
-        """Chunk size giving each resident chain (warp, or lane when ``per_warp`` is 32)
-        about four chunks of the NFA bytes (a power of two in [MIN_CHUNK, 1 MiB])."""
-        per = nfa_bytes // max(1, 4 * self.resident_warps * per_warp)
+    def auto_chunk_bytes(self, nfa_bytes: int) -> int:
+        """Warp chunks: about four per resident warp of the persistent launch (a power of
+        two in [MIN_CHUNK, 1 MiB])."""
+        per = nfa_bytes // max(1, 4 * self.resident_warps)
         size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
         return int(min(size, 1 << 20))
 
-    def _shift_boundaries(self, ch: np.ndarray, inp: np.ndarray, aut: np.ndarray,
-                          data: np.ndarray) -> None:
-        """Move the start of every non-first lane chunk (and the end of its predecessor)
-        forward to the first position in the next BOUNDARY_WINDOW bytes whose two-byte
-        superset holds at most BOUNDARY_SET states (the smallest one if none does): a
-        smaller starting superset converges sooner and rarely outgrows the lane."""
-        later = np.flatnonzero(ch["index"] > 0)
-        if later.size == 0:
-            return
-        span = (ch["end"][later] - ch["begin"][later]).min()
-        w = int(min(BOUNDARY_WINDOW, max(1, span // 4)))
-        for a in np.unique(aut[later]):
-            sizes = self.dev[int(a)].pair_sizes
-            sel = later[aut[later] == a]
-            pos = ch["begin"][sel][:, None] + np.arange(w)[None, :]
-            key = data[pos - 2].astype(np.int64) * 256 + data[pos - 1]
-            sz = sizes[key]
-            ok = sz <= BOUNDARY_SET
-            pick = np.where(ok.any(axis=1), ok.argmax(axis=1), sz.argmin(axis=1))
-            new_begin = ch["begin"][sel] + pick
-            ch["begin"][sel] = new_begin
-            ch["end"][sel - 1] = new_begin
+    def auto_lane_chunk_bytes(self, nfa_bytes: int) -> int:
+        """Lane chunks: about one per resident lane of the lane launch, so that the batch
+        runs in a single wave (the power of two nearest to bytes / lanes, in
+        [MIN_CHUNK, 1 MiB]). A lane's steps are dependent L2 round trips, so splitting
+        finer only adds chunk overhead once every lane is busy."""
+        lanes = self.sm_count * LANE_WARPS_PER_SM * 32
+        per = max(1.0, nfa_bytes / lanes)
+        size = 1 << int(round(np.log2(per)))
+        return int(min(max(size, MIN_CHUNK), 1 << 20))
 
-    def make_tasks(self, aut_ids, lengths, starts=None, data=None) -> TaskPlan:
+    def make_tasks(self, aut_ids, lengths, starts=None) -> TaskPlan:
         """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
-        packed back to back from 0) on automaton ``aut_ids[i]``. ``data`` (host bytes,
-        indexed like ``starts``) lets lane chunks start where the superset is small."""
+        packed back to back from 0) on automaton ``aut_ids[i]``. Chunk bounds are nominal:
+        the kernels move each later chunk's start a few bytes forward to where the
+        two-byte superset is small (chunk_bounds in csrc/chunks.cuh)."""
         aut_ids = np.asarray(aut_ids, dtype=np.int64)
         lengths = np.asarray(lengths, dtype=np.int64)
         n = aut_ids.size
@@ -271,7 +258,7 @@ class PersistentEngine:
                 chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
             else:
                 chunk_w = self.auto_chunk_bytes(int(lengths[warp_in].sum()))
-                chunk_l = self.auto_chunk_bytes(int(lengths[lane_in].sum()), LANE_GROUP)
+                chunk_l = self.auto_lane_chunk_bytes(int(lengths[lane_in].sum()))
             csize[warp_in] = chunk_w
             csize[lane_in] = chunk_l
         # every input of a lane automaton is chunked (a short one is a single exact
@@ -307,9 +294,6 @@ class PersistentEngine:
             ch["begin"] = starts[inp] + idx * ln // cnt
             ch["end"] = starts[inp] + (idx + 1) * ln // cnt
             n_lane = int(counts[:sl.size].sum())
-            if n_lane and data is not None:
-                self._shift_boundaries(ch[:n_lane], inp[:n_lane], aut_ids[inp[:n_lane]],
-                                       np.asarray(data))
             chunk_list.append(ch)
             clen = ch["end"] - ch["begin"]
             # LANES tasks: up to 32 consecutive lane chunks of one automaton
@@ -378,14 +362,23 @@ class PersistentEngine:
         native.check(st, "gbfsm_persistent_run")
 
     def launch(self, d_data, d_off, dt: DeviceTasks, d_flags, d_lens, d_examined=None,
-               stream=None, d_ends=None, workspace=None) -> int:
+               stream=None, d_ends=None, workspace=None, phases: dict | None = None) -> int:
         """Enqueue the batch's launches; returns how many kernels were launched:
         the lane launch (LANES tasks), the persistent launch (WHOLE / CHUNK tasks), the
         overflow pass (lane chunks that outgrew their lane, run by warps) and the fix-up
         (FIXUP tasks), each only when it has work. ``d_data`` is a device tensor or a raw
         device address (e.g. of pinned host memory read in place); with ``d_ends`` input
-        i spans ``[d_off[i], d_ends[i])``."""
+        i spans ``[d_off[i], d_ends[i])``. ``phases`` (optional) collects a pair of timing
+        events around each launch, keyed "lanes", "persistent", "overflow", "fixup"."""
         stream = stream or torch.cuda.current_stream(self.device)
+
+        def mark(name):
+            if phases is None:
+                return None
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            phases.setdefault(name, []).append(e)
+            return e
         ws = self.workspace if workspace is None else workspace
         data_ptr = d_data if isinstance(d_data, int) else d_data.data_ptr()
         base = dt.d_tasks.data_ptr()
@@ -394,22 +387,30 @@ class PersistentEngine:
             with torch.cuda.stream(stream):
                 dt.d_overflow_count.zero_()
             io = dt.chunk_io()
+            mark("lanes")
             st = native.lib().gbfsm_lanes_run(
                 self.table.data_ptr(), len(self.automata), base, dt.nl, data_ptr,
                 d_off.data_ptr(), ctypes.byref(io), stream.cuda_stream)
             native.check(st, "gbfsm_lanes_run")
+            mark("lanes")
             launches += 1
         if dt.na or not (dt.nl or dt.nb):
+            mark("persistent")
             self._run(base + dt.nl * 16, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
                       d_examined, ws, stream)
+            mark("persistent")
             launches += 1
         if dt.nl:
+            mark("overflow")
             self._run(dt.d_overflow.data_ptr(), dt.n_lane_chunks, dt, data_ptr, d_off, d_ends,
                       d_flags, d_lens, d_examined, ws, stream, overflow_pass=True)
+            mark("overflow")
             launches += 1
         if dt.nb:
+            mark("fixup")
             self._run(base + (dt.nl + dt.na) * 16, dt.nb, dt, data_ptr, d_off, d_ends, d_flags,
                       d_lens, d_examined, ws, stream)
+            mark("fixup")
             launches += 1
         return launches
 
@@ -424,7 +425,7 @@ class PersistentEngine:
         stream = torch.cuda.current_stream(self.device)
         lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
         d_data, d_off, _, _ = self._staging.put(inputs, stream)
-        plan = self.make_tasks(np.asarray(aut_ids), lengths, data=self._staging.host_data())
+        plan = self.make_tasks(np.asarray(aut_ids), lengths)
         self._tasks.upload(plan, stream)
         self._results.ensure(max(n, 1))
         res = self._results
@@ -464,14 +465,16 @@ class GraphRunner:
     """
 
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
-                 with_examined: bool = False) -> None:
+                 with_examined: bool = False, zero_copy: bool = False) -> None:
+        """``zero_copy``: the captured graph does not copy the inputs; the kernels read
+        them in place from the pinned host buffer over the host link (NVLink-C2C on
+        GB300). ``kernel_only`` always uses the device copy."""
         self.engine = engine
         dev = engine.device
         n = len(offsets) - 1
         self.n = n
         lengths = np.diff(np.asarray(offsets, dtype=np.int64))
-        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths,
-                                           data=np.asarray(data, dtype=np.uint8))
+        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths)
         total = int(offsets[-1])
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
@@ -479,7 +482,10 @@ class GraphRunner:
         self.h_off = torch.from_numpy(np.asarray(offsets, dtype=np.int64).copy()).pin_memory()
         self.h_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, pin_memory=True)
         self.d_data = torch.empty_like(self.h_data, device=dev)
+        self.d_data.copy_(self.h_data)
         self.d_off = torch.empty_like(self.h_off, device=dev)
+        self.zero_copy = zero_copy
+        self.host_ptr = native.device_pointer(self.h_data.data_ptr()) if zero_copy else None
         self.d_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, device=dev)
         self.tasks = DeviceTasks(dev)
         self.with_examined = with_examined
@@ -502,24 +508,25 @@ class GraphRunner:
 
     def _body(self) -> None:
         s = torch.cuda.current_stream(self.engine.device)
-        self.d_data.copy_(self.h_data, non_blocking=True)
+        if not self.zero_copy:
+            self.d_data.copy_(self.h_data, non_blocking=True)
         self.d_off.copy_(self.h_off, non_blocking=True)
         self.tasks.upload(self.task_plan, s)
         self.launches_per_step = self.engine.launch(
-            self.d_data, self.d_off, self.tasks, self.d_out[0], self.d_out[1],
-            self.d_out[2] if self.with_examined else None, s)
+            self.host_ptr if self.zero_copy else self.d_data, self.d_off, self.tasks,
+            self.d_out[0], self.d_out[1], self.d_out[2] if self.with_examined else None, s)
         self.h_out.copy_(self.d_out, non_blocking=True)
 
     def replay(self) -> None:
         """Launch the captured graph (asynchronous)."""
         self.graph.replay()
 
-    def kernel_only(self, stream=None) -> int:
+    def kernel_only(self, stream=None, phases: dict | None = None) -> int:
         """The launches alone on resident inputs (for device-side timing)."""
         stream = stream or torch.cuda.current_stream(self.engine.device)
         return self.engine.launch(self.d_data, self.d_off, self.tasks, self.d_out[0],
                                   self.d_out[1], self.d_out[2] if self.with_examined else None,
-                                  stream)
+                                  stream, phases=phases)
 
     def verdicts(self):
         h = self.h_out.numpy()

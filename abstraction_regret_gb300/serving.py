@@ -118,7 +118,7 @@ class Server:
         a = aut_ids[reqs]
         ln = lengths[reqs]
         if self.zero_copy:
-            plan = self.engine.make_tasks(a, ln, starts[reqs], data=pool)
+            plan = self.engine.make_tasks(a, ln, starts[reqs])
             off = slot.h_off.numpy()
             off[:n] = starts[reqs]
             off[n:2 * n] = starts[reqs] + ln
@@ -133,7 +133,7 @@ class Server:
                 h[pos:pos + k] = pool[s:s + k]
                 pos += k
             h[pos:pos + PAD] = 0
-            plan = self.engine.make_tasks(a, ln, data=h)
+            plan = self.engine.make_tasks(a, ln)
         with torch.cuda.stream(slot.stream):
             if self.zero_copy:
                 slot.d_off[:2 * n].copy_(slot.h_off[:2 * n], non_blocking=True)

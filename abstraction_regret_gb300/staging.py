@@ -73,10 +73,6 @@ class Staging:
             self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
         return self._d_data[:padded], self._d_off[: n + 1], h_off, total
 
-    def host_data(self) -> np.ndarray:
-        """The pinned host copy of the last batch (valid until the next ``put``)."""
-        return self._h_data.numpy()
-
     def put_flat(self, data: np.ndarray, offsets: np.ndarray, stream: torch.cuda.Stream):
         """Like ``put`` for an already flat uint8 batch with int64 offsets."""
         n = len(offsets) - 1

@@ -11,15 +11,20 @@ examined (the literal configuration's uniform bytes kill the active set after ab
 byte). Inputs are larger than L2 (261 MB > 129 MB).
 
 Printed (rank 0, one JSON line):
-  value       GB/s of input through the persistent launch, inputs resident in HBM
-              (CUDA events around K launches on the launching stream);
+  value       GB/s of input through the engine's launches (lane launch, persistent
+              launch, overflow pass, fix-up), inputs resident in HBM (CUDA events
+              around K steps on the launching stream);
   e2e         the same batch through the public engine path: a captured CUDA graph
-              that copies the inputs host->device from pinned memory, runs the
-              persistent launch and copies the verdicts back, every step;
+              that moves the inputs from pinned host memory (read in place over
+              NVLink-C2C by the kernels; ``e2e_copy``: copied host->device first), runs
+              the launches and copies the verdicts back, every step;
   plain_*     the plain kernels on the same batch: one launch per input (sample,
               sequential on one stream, scaled by bytes) and one launch for the batch;
   dfa         the plain DFA walk on the c2 configuration (4096 states, 4096 x 64 KiB);
-  roofline    the persistent kernel against the measured HBM copy bandwidth;
+  serving     the continuous-batching loop on the c5 trace (p50 / p99 latency, offered
+              GB/s, against one plain launch per request);
+  roofline    the dominant kernel (the lane launch) against the measured HBM copy
+              bandwidth, with an L2 view beside it;
   cpu_baseline the CPU oracle port on this host's cores on a bounded sample.
 
 With ``--impl reference`` the reference's CPU algorithm (the C port of
@@ -56,7 +61,11 @@ def parse_args(argv=None):
     ap.add_argument("--workload", default="c3-sustained",
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
-                    help="only the headline persistent measurement (used for profiling)")
+                    help="only the headline measurement (used for profiling)")
+    ap.add_argument("--serve-requests", type=int, default=20000,
+                    help="requests of the c5 serving trace (0: skip the serving section)")
+    ap.add_argument("--slo-ms", type=float, default=50.0,
+                    help="p99 latency objective of the serving section")
     return ap.parse_args(argv)
 
 
@@ -154,35 +163,26 @@ def time_launches(fn, stream, steps: int, warmup: int):
 
 
 def cpu_reference(batch, budget_s: float = 15.0, threads: int | None = None):
-    """The oracle port on this host: a bounded prefix (shortest-first) sample."""
+    """The oracle port on this host's cores: whole passes over the batch (inputs spread
+    over all threads) until ``budget_s`` of wall time has gone; at least one pass."""
     from oracle import oracle as O
 
     threads = threads or os.cpu_count() or 1
     a = batch.automata[0]
-    lens = np.diff(batch.offsets)
-    order = np.argsort(lens, kind="stable")
-    # calibrate on a small sample, then size the sample to the time budget
-    take = order[: max(threads, 8)]
-    sub = batch.subset(np.sort(take))
+    passes, examined = 0, 0
     t0 = time.perf_counter()
-    O.nfa_batch(a, sub.data, sub.offsets, threads)
-    dt = time.perf_counter() - t0
-    rate = max(sub.total_bytes / max(dt, 1e-6), 1e6)
-    target = rate * budget_s * 0.5
-    idx, acc = [], 0
-    for i in order[::max(1, len(order) // 256)]:
-        if acc + lens[i] > target:
-            continue
-        idx.append(int(i))
-        acc += int(lens[i])
-    sub = batch.subset(np.sort(np.asarray(idx)))
-    t0 = time.perf_counter()
-    _, _, ex, _ = O.nfa_batch(a, sub.data, sub.offsets, threads)
-    dt = time.perf_counter() - t0
-    return {"value": sub.total_bytes / dt / 1e9, "unit": "GB/s", "cores": int(threads),
-            "kind": "port",
-            "sample": f"{sub.n_inputs} of {batch.n_inputs} inputs ({sub.total_bytes / 1e6:.1f} MB, "
-                      f"{int(ex.sum()) / 1e6:.1f} MB examined), {dt:.1f} s"}
+    while True:
+        _, _, ex, _ = O.nfa_batch(a, batch.data, batch.offsets, threads)
+        passes += 1
+        examined += int(ex.sum())
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            break
+    return {"value": passes * batch.total_bytes / dt / 1e9, "unit": "GB/s",
+            "cores": int(threads), "kind": "port",
+            "sample": f"{passes} whole passes over the {batch.n_inputs}-input batch "
+                      f"({passes * batch.total_bytes / 1e6:.0f} MB offered, "
+                      f"{examined / 1e6:.0f} MB examined) in {dt:.1f} s"}
 
 
 def run_reference(args, world, rank):
@@ -193,7 +193,7 @@ def run_reference(args, world, rank):
     samples = []
     info = None
     for i in range(args.warmup + args.steps):
-        info = cpu_reference(batch, budget_s=8.0)
+        info = cpu_reference(batch, budget_s=10.0 if i >= args.warmup else 1.0)
         if i >= args.warmup:
             samples.append(info["value"])
     value = float(np.median(samples))
@@ -238,38 +238,57 @@ def main(argv=None) -> int:
     nfa = batch.automata[0]
     eng = PersistentEngine([nfa], dev)
     runner = GraphRunner(eng, batch.aut_ids, batch.data, batch.offsets, with_examined=True)
+    zrunner = GraphRunner(eng, batch.aut_ids, batch.data, batch.offsets, with_examined=True,
+                          zero_copy=True)
     stream = runner.stream
 
-    # ---- oracle gate before any timing (full batch, bit-exact) ----------------------------
-    with torch.cuda.stream(stream):
-        runner.replay()
-    stream.synchronize()
-    flags, lens, examined = runner.verdicts()
+    # ---- oracle gate before any timing (full batch, bit-exact, both ingest paths) ----------
+    verdicts = []
+    for r in (runner, zrunner):
+        with torch.cuda.stream(r.stream):
+            r.replay()
+        r.stream.synchronize()
+        verdicts.append(r.verdicts())
+    flags, lens, examined = verdicts[0]
     gate = {"checked": 0}
     if rank == 0:
         from oracle import oracle as O
 
-        f, l, ex, _, work = O.nfa_batch(nfa, batch.data, batch.offsets, with_work=True)
-        if not (np.array_equal(flags, f) and np.array_equal(lens, l) and np.array_equal(examined, ex)):
-            bad = np.flatnonzero((flags != f) | (lens != l))
-            raise SystemExit(f"oracle gate failed on {bad.size} inputs (first {bad[:5].tolist()})")
-        gate = {"checked": int(flags.size), "accepted": int(f.sum()),
-                "examined_bytes": int(ex.sum()), "edges_scanned": int(work.sum())}
+        f, l, ex, _, work, visits = O.nfa_batch(nfa, batch.data, batch.offsets, with_work=True)
+        for fl, le, exa in verdicts:
+            if not (np.array_equal(fl, f) and np.array_equal(le, l) and np.array_equal(exa, ex)):
+                bad = np.flatnonzero((fl != f) | (le != l) | (exa != ex))
+                raise SystemExit(f"oracle gate failed on {bad.size} inputs "
+                                 f"(first {bad[:5].tolist()})")
+        gate = {"checked": int(flags.size), "paths": ["device copy", "zero-copy"],
+                "accepted": int(f.sum()), "examined_bytes": int(ex.sum()),
+                "edges_scanned": int(work.sum()), "states_stepped": int(visits.sum())}
 
     offered = batch.total_bytes
     examined_bytes = int(examined.sum())
 
-    # ---- headline: persistent launch on resident inputs --------------------------------
+    # ---- headline: the engine's launches on resident inputs ------------------------------
     def barrier():
         if world > 1:
             dist.barrier()
 
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            runner.kernel_only(stream)
+    phases: dict = {}
     barrier()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
-            ms = time_launches(runner.kernel_only, stream, args.steps, args.warmup)
-        launches = runner.launches_per_step * args.steps
+            e0.record(stream)
+            launches = 0
+            for _ in range(args.steps):
+                launches += runner.kernel_only(stream, phases=phases)
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
         torch.cuda.synchronize()
     barrier()
     if world > 1:
@@ -277,17 +296,28 @@ def main(argv=None) -> int:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = offered * world / (ms * 1e-3) / 1e9
+    phase_ms = {k: float(np.mean([ev[2 * i].elapsed_time(ev[2 * i + 1])
+                                  for i in range(len(ev) // 2)]))
+                for k, ev in phases.items()}
 
-    # ---- e2e: graph replay with H2D inputs and D2H verdicts every step --------------------
-    with torch.cuda.stream(stream):
-        e2e_ms = time_launches(runner.replay, stream, args.steps, args.warmup)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": offered * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-           "h2d_bytes_per_step": int(runner.h2d_bytes), "d2h_bytes_per_step": int(runner.d2h_bytes),
-           "ms_per_step": e2e_ms, "path": "CUDA graph: pinned H2D + persistent launch + D2H"}
+    # ---- e2e: graph replay, inputs from pinned host memory, verdicts back every step ----
+    e2e_ms = {}
+    for name, r in (("zero_copy", zrunner), ("copy", runner)):
+        with torch.cuda.stream(r.stream):
+            e2e_ms[name] = time_launches(r.replay, r.stream, args.steps, args.warmup)
+        if world > 1:
+            t = torch.tensor([e2e_ms[name]], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms[name] = float(t.item())
+    e2e = {"value": offered * world / (e2e_ms["zero_copy"] * 1e-3) / 1e9, "unit": "GB/s",
+           "h2d_bytes_per_step": int(zrunner.h2d_bytes),
+           "d2h_bytes_per_step": int(zrunner.d2h_bytes), "ms_per_step": e2e_ms["zero_copy"],
+           "path": "CUDA graph: tables H2D, kernels read the inputs from pinned host memory "
+                   "over NVLink-C2C, verdicts D2H"}
+    e2e_copy = {"value": offered * world / (e2e_ms["copy"] * 1e-3) / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": int(runner.h2d_bytes),
+                "d2h_bytes_per_step": int(runner.d2h_bytes), "ms_per_step": e2e_ms["copy"],
+                "path": "CUDA graph: inputs + tables H2D from pinned memory, launches, D2H"}
 
     extras = {}
     if not args.skip_extras and rank == 0:
@@ -322,6 +352,7 @@ def main(argv=None) -> int:
                                      "note": "one launch per input, sequential on one stream"}
         extras["speedup_vs_plain_per_input"] = value / world / per_input_gbps
         extras["speedup_vs_plain_single_launch"] = value / world / extras["plain_single_launch"]["value"]
+        del plain, d_out
         # DFA walk on c2 (literal and sustained)
         for variant in ("literal", "sustained"):
             b2 = W.c2(variant)
@@ -338,33 +369,46 @@ def main(argv=None) -> int:
                 "examined_GBps": int(oe.sum()) / (d_ms * 1e-3) / 1e9,
                 "ms": d_ms, "examined_bytes": int(oe.sum()), "checked": int(of.size)}
             del r2, ex2, b2
+        if args.serve_requests > 0:
+            extras["serving"] = serving_section(dev, args.serve_requests, args.slo_ms)
 
     cpu = cpu_reference(batch) if rank == 0 else None
 
-    # ---- roofline of the persistent kernel -------------------------------------------
+    # ---- roofline of the dominant kernel ----------------------------------------------
     peaks = {}
     try:
         peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    # algorithmic bytes: 1 input byte per examined symbol + one 16-byte edge record per
-    # symbol edge scanned (the oracle counts them exactly), + 12 bytes of results per input
-    algo = gate.get("examined_bytes", examined_bytes) + 16 * gate.get("edges_scanned", 0) + \
-        12 * batch.n_inputs
-    achieved = algo / (ms * 1e-3) / 1e9
+    top = max(phase_ms, key=phase_ms.get) if phase_ms else "lanes"
+    kernel_ms = phase_ms.get(top, ms)
+    kernel_name = {"lanes": "lanes_kernel", "persistent": "persistent_kernel",
+                   "overflow": "persistent_kernel", "fixup": "persistent_kernel"}[top]
+    # algorithmic bytes of the exact simulation (CSR view): per examined symbol 1 input
+    # byte, per active state an 8-byte row range, per scanned edge 8 bytes (symbol +
+    # target); 12 bytes of verdicts per input. Counted by the oracle on the same batch.
+    algo = gate.get("examined_bytes", examined_bytes) + 8 * gate.get("states_stepped", 0) + \
+        8 * gate.get("edges_scanned", 0) + 12 * batch.n_inputs
+    achieved = algo / (kernel_ms * 1e-3) / 1e9
     traffic = None  # DRAM bytes per launch from the committed ncu summary, when one exists
     tpath = REPO / "profiles" / "traffic.txt"
     if tpath.exists():
         for line in tpath.read_text().splitlines():
             parts = line.split()
-            if len(parts) == 3 and parts[0] == "persistent_kernel" and parts[1] == args.workload:
+            if len(parts) == 3 and parts[0] == kernel_name and parts[1] == args.workload:
                 traffic = int(parts[2])
+    l2 = l2_copy_gbs(dev)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                "kernel": "persistent_kernel",
-                "algorithmic_bytes_per_launch": int(algo)}
+                "kernel": kernel_name, "kernel_ms": kernel_ms,
+                "algorithmic_bytes_per_launch": int(algo),
+                "input_stream": {"achieved": examined_bytes / (kernel_ms * 1e-3) / 1e9,
+                                 "frac": examined_bytes / (kernel_ms * 1e-3) / 1e9 / hbm},
+                "l2": {"peak": l2, "frac": achieved / l2 if l2 else None,
+                       "peak_source": "measured here: L2-resident elementwise copy kernel, "
+                                      "2 x 24 MiB"}}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
@@ -377,16 +421,90 @@ def main(argv=None) -> int:
                            "offered_bytes": offered, "examined_bytes": examined_bytes,
                            "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}",
-                           "technique": "persistent, speculative chunks of "
-                                        f"{runner.task_plan.chunk_bytes} B "
-                                        f"({runner.task_plan.chunks.shape[0]} chunks)"},
-                "e2e": e2e, "gpu_launches": launches, "oracle_gate": gate,
+                           "technique": f"lane chunks of {runner.task_plan.lane_chunk_bytes} B "
+                                        f"({runner.task_plan.lane_chunks} of "
+                                        f"{runner.task_plan.chunks.shape[0]} chunks), "
+                                        "overlap-linked parallel fix-up"},
+                "phases_ms": phase_ms,
+                "e2e": e2e, "e2e_copy": e2e_copy, "gpu_launches": launches, "oracle_gate": gate,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def l2_copy_gbs(dev) -> float | None:
+    """Read+write GB/s of an L2-resident elementwise copy kernel (2 x 24 MiB, best of 20,
+    CUDA events)."""
+    import torch
+
+    try:
+        a = torch.ones(6 << 20, dtype=torch.int32, device=dev)
+        b = torch.empty_like(a)
+        best = float("inf")
+        for _ in range(20):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                torch.mul(a, 1, out=b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 10)
+        return 2 * a.numel() * 4 / (best * 1e-3) / 1e9
+    except RuntimeError:
+        return None
+
+
+def serving_section(dev, n_requests: int, slo_ms: float) -> dict:
+    """c5: the serving loop over the resident 32-automaton pool at swept arrival rates,
+    against one plain launch per request; verdicts equal to the plain path on every
+    request and to the oracle on a sample."""
+    import torch
+
+    from abstraction_regret_gb300 import workloads as W
+    from abstraction_regret_gb300.engine import PersistentEngine
+    from abstraction_regret_gb300.executors import make_dfa_executor, make_nfa_executor
+    from abstraction_regret_gb300.serving import Server, serve_plain
+    from oracle import oracle as O
+
+    pool = W.c5_pool()
+    engine = PersistentEngine(pool, dev)
+    out = {"pool": "16 NFAs (c4 distribution) + 16 DFAs (1024..16384 states)",
+           "requests": n_requests, "slo_p99_ms": slo_ms, "rates": []}
+    base = W.c5(rate_per_s=1.0, n_requests=n_requests, automata=pool)
+    pinned = torch.from_numpy(base.pool).pin_memory()
+    # plain baseline: one launch per request, arrivals ignored (back to back)
+    ex = {k: (make_dfa_executor(a, "gather") if hasattr(a, "trans") else
+              make_nfa_executor(a, "compact")) for k, a in enumerate(pool)}
+    pf, pl, plat, pstats = serve_plain(engine, base, ex, time_scale=0.0)
+    out["plain_per_request"] = {"offered_GBps": pstats.offered_GBps, "wall_s": pstats.wall_s,
+                                "note": "one plain launch per request, back to back"}
+    # oracle on a sample of requests
+    rng = np.random.default_rng(0)
+    sample = rng.choice(n_requests, min(400, n_requests), replace=False)
+    for i in sample:
+        a, data = base.request(int(i))
+        want = O.verdicts(pool[a], [bytes(data)])[0]
+        if (int(pf[i]), int(pl[i])) != (int(want[0]), int(want[1])):
+            raise SystemExit(f"serving: plain path disagrees with the oracle on request {i}")
+    # swept Poisson rates, then every request at once (the loop's saturation throughput)
+    for rate in (2000.0, 8000.0, 32000.0, 128000.0, None):
+        tr = W.c5(rate_per_s=rate or 1.0, n_requests=n_requests, automata=pool)
+        srv = Server(engine=engine, slots=3, batch_bytes=256 << 20, max_requests=4096,
+                     zero_copy=True)
+        f, l, lat, st = srv.serve(tr, time_scale=1.0 if rate else 0.0, pinned_pool=pinned)
+        if not (np.array_equal(f, pf) and np.array_equal(l, pl)):
+            raise SystemExit(f"serving at {rate}/s: verdicts differ from the plain path")
+        d = st.as_dict()
+        d.update({"rate_per_s": rate if rate else "all at t=0",
+                  "slo_met": bool(st.p99_ms <= slo_ms)})
+        out["rates"].append(d)
+        del srv
+    out["checked"] = {"plain_equal": n_requests, "oracle_sample": int(sample.size)}
+    return out
 
 
 class GraphRunnerLike:

@@ -31,7 +31,9 @@
  *                 what a "divergence > 1" input filter looks at;
  *   work[i]       symbol edges scanned over the run (the sum over consumed bytes of the
  *                 out-degrees of the active states), which sizes a simulator's edge
- *                 traffic per byte.
+ *                 traffic per byte;
+ *   visits[i]     active states stepped over the run (the sum over consumed bytes of the
+ *                 active-set size), which sizes its row-pointer traffic.
  *
  * Sets are a membership byte map plus a member list (O(1) insert, O(|set|) iteration
  * and clear), so a run costs O(edges touched), like the reference's Python sets.
@@ -85,8 +87,8 @@ static int closure(const nfa_t *a, int32_t *list, int32_t *count, uint8_t *in, i
 
 static void nfa_one(const nfa_t *a, scratch_t *w, const uint8_t *data, int64_t len,
                     int32_t *flag, int32_t *mlen, int64_t *examined, int32_t *max_active,
-                    int64_t *work) {
-    int64_t edges = 0;
+                    int64_t *work, int64_t *visits) {
+    int64_t edges = 0, stepped = 0;
     int32_t nc = 0, nn = 0, peak;
     w->cur[nc++] = a->start;
     w->in_cur[a->start] = 1;
@@ -101,6 +103,7 @@ static void nfa_one(const nfa_t *a, scratch_t *w, const uint8_t *data, int64_t l
         for (i = 0; i < len; ++i) {
             int32_t b = data[i];
             nn = 0;
+            stepped += nc;
             for (int32_t j = 0; j < nc; ++j) {
                 int32_t s = w->cur[j];
                 edges += a->srp[s + 1] - a->srp[s];
@@ -143,6 +146,7 @@ static void nfa_one(const nfa_t *a, scratch_t *w, const uint8_t *data, int64_t l
     if (examined) *examined = ex;
     if (max_active) *max_active = peak;
     if (work) *work = edges;
+    if (visits) *visits = stepped;
 }
 
 /* Reject automata the simulator would index out of bounds with. Returns 0 when valid. */
@@ -170,7 +174,7 @@ typedef struct {
     int64_t n_inputs;
     int64_t next; /* shared work counter */
     int32_t *flags, *lens, *max_active;
-    int64_t *examined, *work;
+    int64_t *examined, *work, *visits;
     int failed;
 } job_t;
 
@@ -192,7 +196,8 @@ static void *nfa_worker(void *arg) {
             nfa_one(a, &w, job->data + job->offsets[i], job->offsets[i + 1] - job->offsets[i],
                     &job->flags[i], &job->lens[i], job->examined ? &job->examined[i] : NULL,
                     job->max_active ? &job->max_active[i] : NULL,
-                    job->work ? &job->work[i] : NULL);
+                    job->work ? &job->work[i] : NULL,
+                    job->visits ? &job->visits[i] : NULL);
         }
     }
     free(w.in_cur); free(w.in_nxt); free(w.cur); free(w.nxt); free(w.stack);
@@ -266,7 +271,7 @@ int fsm_oracle_nfa_batch(int32_t num_states, int32_t start_state, const uint8_t 
                          const int32_t *eps_targets, const uint8_t *data,
                          const int64_t *offsets, int64_t n_inputs, int32_t n_threads,
                          int32_t *flags, int32_t *lens, int64_t *examined,
-                         int32_t *max_active, int64_t *work) {
+                         int32_t *max_active, int64_t *work, int64_t *visits) {
     nfa_t a = {num_states, start_state, accept, sym_row_ptr, sym_targets, sym_symbols,
                eps_row_ptr, eps_targets};
     if (nfa_valid(&a) != 0 || offsets_valid(offsets, n_inputs) != 0) return -1;
@@ -281,6 +286,7 @@ int fsm_oracle_nfa_batch(int32_t num_states, int32_t start_state, const uint8_t 
     job.examined = examined;
     job.max_active = max_active;
     job.work = work;
+    job.visits = visits;
     return run_pool(&job, n_threads, nfa_worker);
 }
 

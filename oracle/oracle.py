@@ -118,7 +118,8 @@ def _load():
         p = ctypes.c_void_p
         lib.fsm_oracle_nfa_batch.restype = ctypes.c_int
         lib.fsm_oracle_nfa_batch.argtypes = [ctypes.c_int32, ctypes.c_int32, p, p, p, p, p, p, p,
-                                             p, ctypes.c_int64, ctypes.c_int32, p, p, p, p, p]
+                                             p, ctypes.c_int64, ctypes.c_int32, p, p, p, p, p,
+                                             p]
         lib.fsm_oracle_dfa_batch.restype = ctypes.c_int
         lib.fsm_oracle_dfa_batch.argtypes = [ctypes.c_int32, ctypes.c_int32, p, p, p, p,
                                              ctypes.c_int64, ctypes.c_int32, p, p, p]
@@ -146,7 +147,8 @@ def _threads(threads: int | None) -> int:
 def nfa_batch(nfa, data: np.ndarray, offsets: np.ndarray, threads: int | None = None,
               with_work: bool = False):
     """C oracle over a flat batch. Returns ``(flags, lens, examined, max_active)``, plus
-    ``work`` (symbol edges scanned per input) when ``with_work``."""
+    ``work`` (symbol edges scanned per input) and ``visits`` (active states stepped per
+    input) when ``with_work``."""
     lib = _load()
     n_in = len(offsets) - 1
     acc = np.ascontiguousarray(nfa.accept, dtype=np.uint8)
@@ -159,14 +161,15 @@ def nfa_batch(nfa, data: np.ndarray, offsets: np.ndarray, threads: int | None = 
     examined = np.zeros(n_in, np.int64)
     peak = np.zeros(n_in, np.int32)
     work = np.zeros(n_in, np.int64)
+    visits = np.zeros(n_in, np.int64)
     rc = lib.fsm_oracle_nfa_batch(int(nfa.num_states), int(nfa.start_state), _ptr(acc),
                                   *[_ptr(a) for a in arrs], _ptr(data), _ptr(offsets), n_in,
                                   _threads(threads), _ptr(flags), _ptr(lens), _ptr(examined),
-                                  _ptr(peak), _ptr(work))
+                                  _ptr(peak), _ptr(work), _ptr(visits))
     if rc != 0:
         raise ValueError(f"oracle rejected the automaton or offsets (rc={rc})")
     if with_work:
-        return flags, lens, examined, peak, work
+        return flags, lens, examined, peak, work, visits
     return flags, lens, examined, peak
 
 
