@@ -4,7 +4,7 @@
 // An input is cut into chunks. Its first chunk runs exactly from the start configuration.
 // Every later chunk starting at byte b runs from a superset of the true active set at b:
 // the targets of every edge labelled x[b-2] (or ANY), stepped over x[b-1] (for automata
-// without epsilon edges this two-byte superset is tabulated, pair_edges). Because
+// without epsilon edges this two-byte superset is tabulated, pair_lanes). Because
 // simulation preserves set inclusion, the speculative set contains the true set at every
 // later position of the chunk, so equal sizes mean equal sets. The chunk records its set
 // sizes after 1, 2, 4, ..., 32 bytes, the first accept strictly after each of those
@@ -247,50 +247,104 @@ __device__ inline void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpSc
 
 // ---- lane chunk (one chunk per thread; up to kLaneSlots states) ----------------------------
 //
-// The set is kept as the records of its members (slot q valid when bit q of `valid` is
-// set). Per byte: scan the members' edge labels (uint16, L1-resident) for the byte,
-// collecting at most kLaneSlots matching edges; load their records together (one L2 round
-// trip); the deduplicated targets are the next set.
+// The set is kept as the lane records (gbfsm_lane_rec) of its members, slot q valid when
+// bit q of `valid` is set. Per byte: find each member's edges labelled with the byte --
+// two byte-wise compares of its packed labels for a state in the fast form, a scan of
+// edge_sym (L1-resident) otherwise -- collecting at most kLaneSlots matching edges; load
+// the lane records of their targets together (one L2 round trip); the distinct targets
+// are the next set.
+
+__device__ __forceinline__ uint4 ld_lane(const gbfsm_lane_rec *p) {
+    return __ldg(reinterpret_cast<const uint4 *>(p));
+}
+
+// Lane record of state s, built from the CSR rows (the start state of a first chunk).
+__device__ inline uint4 lane_record_of(const gbfsm_nfa_dev &A, uint32_t s) {
+    const uint32_t rb = __ldg(A.sym_row + s), re = __ldg(A.sym_row + s + 1);
+    const uint32_t deg = re - rb;
+    const bool acc =
+        (__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
+         (s & 63u)) & 1ull;
+    bool slow = deg > 8u;
+    uint32_t lo = 0, hi = 0;
+    for (uint32_t j = 0; j < deg && !slow; ++j) {
+        const uint32_t sym = __ldg(A.edge_sym + rb + j);
+        if (sym == (uint32_t)GBFSM_ANY_SYMBOL) slow = true;
+        if (j < 4) lo |= (sym & 0xFFu) << (8u * j);
+        else hi |= (sym & 0xFFu) << (8u * (j - 4));
+    }
+    const uint32_t x = s | (slow ? 0u : deg << GBFSM_LANE_DEG_SHIFT) |
+                       (slow ? GBFSM_LANE_SLOW : 0u) | (acc ? GBFSM_LANE_ACCEPT : 0u);
+    return slow ? make_uint4(x, rb, re, 0u) : make_uint4(x, rb, lo, hi);
+}
+
+// The engine state record (as WarpNfa keeps it) of a lane record.
+__device__ __forceinline__ uint4 warp_record_of(uint4 l) {
+    const uint32_t deg = (l.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
+    const uint32_t re = (l.x & GBFSM_LANE_SLOW) ? l.z : l.y + deg;
+    return make_uint4(l.x & GBFSM_LANE_STATE_MASK,
+                      (l.x & GBFSM_LANE_ACCEPT) ? GBFSM_EDGE_ACCEPT : 0u, l.y, re);
+}
+
+// Append edge k to the match list (kept in registers: the index is a run-time count).
+__device__ __forceinline__ void add_match(uint32_t (&mk)[kLaneSlots], int &nm, uint32_t k) {
+#pragma unroll
+    for (int u = 0; u < kLaneSlots; ++u)
+        if (u == nm) mk[u] = k;
+    ++nm;
+}
 
 // One byte: returns the new member count (acc: a member accepts), or -1 when more than
 // kLaneSlots edges match.
 __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
                                          uint32_t sym, const uint16_t *__restrict__ labels,
-                                         const gbfsm_edge *__restrict__ edges) {
+                                         const gbfsm_lane_rec *__restrict__ recs) {
     uint32_t mk[kLaneSlots];
     int nm = 0;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0;
+    const uint32_t sym4 = sym * 0x01010101u;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) {
-        if ((valid >> q) & 1u) {
-            const uint32_t ke = cur[q].w;
-#pragma unroll 4
-            for (uint32_t k = cur[q].z; k < ke; ++k) {
+        if (!((valid >> q) & 1u)) continue;
+        const uint4 r = cur[q];
+        if (!(r.x & GBFSM_LANE_SLOW)) {
+            const uint32_t deg = (r.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
+            // byte-wise equality, limited to the first deg labels
+            uint32_t m_lo = __vcmpeq4(r.z, sym4) & 0x80808080u;
+            uint32_t m_hi = __vcmpeq4(r.w, sym4) & 0x80808080u;
+            m_lo &= deg >= 4u ? 0xFFFFFFFFu : (1u << (8u * deg)) - 1u;
+            m_hi &= deg >= 8u ? 0xFFFFFFFFu : deg <= 4u ? 0u : (1u << (8u * (deg - 4u))) - 1u;
+            while (m_lo) {
+                add_match(mk, nm, r.y + ((uint32_t)(__ffs(m_lo) - 1) >> 3));
+                m_lo &= m_lo - 1u;
+            }
+            while (m_hi) {
+                add_match(mk, nm, r.y + 4u + ((uint32_t)(__ffs(m_hi) - 1) >> 3));
+                m_hi &= m_hi - 1u;
+            }
+        } else {
+            for (uint32_t k = r.y; k < r.z; ++k) {
                 const uint32_t es = __ldg(labels + k);
-                if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) {
-#pragma unroll
-                    for (int u = 0; u < kLaneSlots; ++u)
-                        if (u == nm) mk[u] = k;
-                    ++nm;
-                }
+                if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) add_match(mk, nm, k);
             }
         }
     }
     if (nm > kLaneSlots) return -1;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q)
-        cur[q] = (q < nm) ? ld_edge(edges + mk[q]) : make_uint4(0, 0, 0, 0);
+        cur[q] = (q < nm) ? ld_lane(recs + mk[q]) : make_uint4(0, 0, 0, 0);
     valid = 0;
     acc = false;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) {
         bool keep = q < nm;
 #pragma unroll
-        for (int u = 0; u < q; ++u) keep = keep && (cur[u].x != cur[q].x);
+        for (int u = 0; u < q; ++u)
+            keep = keep && ((cur[u].x ^ cur[q].x) & GBFSM_LANE_STATE_MASK) != 0u;
         if (keep) {
             valid |= 1u << q;
-            acc |= (cur[q].y & GBFSM_EDGE_ACCEPT) != 0;
+            acc |= (cur[q].x & GBFSM_LANE_ACCEPT) != 0u;
         }
     }
     return __popc(valid);
@@ -314,14 +368,9 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
     int32_t dead_at = -1;
     bool stopped = false;
     if (index == 0) {
-        const uint32_t s = (uint32_t)A.start_state;
-        const bool acc =
-            (__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
-             (s & 63u)) & 1ull;
-        cur[0] = make_uint4(s, acc ? GBFSM_EDGE_ACCEPT : 0u, __ldg(A.sym_row + s),
-                            __ldg(A.sym_row + s + 1));
+        cur[0] = lane_record_of(A, (uint32_t)A.start_state);
         valid = 1;
-        if (acc) {
+        if (cur[0].x & GBFSM_LANE_ACCEPT) {
             acc_after[0] = 0;
             stopped = true;
         }
@@ -332,7 +381,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         if (cnt > (uint32_t)kLaneSlots) return false;
 #pragma unroll
         for (int q = 0; q < kLaneSlots; ++q)
-            if ((uint32_t)q < cnt) cur[q] = ld_edge(A.pair_edges + pr + q);
+            if ((uint32_t)q < cnt) cur[q] = ld_lane(A.pair_lanes + pr + q);
         valid = (1u << cnt) - 1u;
         if (cnt == 0) {
             dead_at = (int32_t)b;
@@ -340,7 +389,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         }
     }
     const uint16_t *__restrict__ labels = A.edge_sym;
-    const gbfsm_edge *__restrict__ edges = A.sym_edges;
+    const gbfsm_lane_rec *__restrict__ recs = A.lane_edges;
     const int64_t len = e - b;
     ByteStream bytes;
     bytes.init(base + b, stopped ? 0 : len);
@@ -350,7 +399,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         const uint32_t sym = bytes.next();
         ++j;
         bool acc;
-        m = lane_step(cur, valid, acc, sym, labels, edges);
+        m = lane_step(cur, valid, acc, sym, labels, recs);
         if (m < 0) return false;
         const int32_t pos = (int32_t)(b + j);
         if (m == 0) {  // reference.py:59-60
@@ -389,13 +438,13 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
 #pragma unroll
         for (int q = 0; q < kLaneSlots; ++q) {
             if ((valid >> q) & 1u) {
-                rec->end_recs[o] = cur[q];
+                rec->end_recs[o] = warp_record_of(cur[q]);
                 ++o;
             }
         }
         for (int64_t t = 1; t <= ov_end - e; ++t) {
             bool acc;
-            const int nm = lane_step(cur, valid, acc, byte_at(base + e + t - 1), labels, edges);
+            const int nm = lane_step(cur, valid, acc, byte_at(base + e + t - 1), labels, recs);
             if (nm < 0) break;
             ov_len = (int32_t)t;
             if (nm == 0) {

@@ -34,6 +34,15 @@ def _padded(n_elems: int, elem_bytes: int, device, dtype=torch.uint8) -> torch.T
     return torch.zeros(nbytes // itemsize, dtype=dtype, device=device)
 
 
+def _records(recs: np.ndarray, device) -> torch.Tensor:
+    """uint32[k, 4] records as a 16-byte-aligned device buffer (at least one record)."""
+    buf = _padded(max(1, recs.shape[0]), 16, device)
+    if recs.size:
+        buf[: recs.nbytes].copy_(torch.from_numpy(np.ascontiguousarray(recs, dtype=np.uint32)
+                                                  .view(np.uint8).ravel()))
+    return buf
+
+
 def _to_dev(a: np.ndarray, dtype, device) -> torch.Tensor:
     arr = np.ascontiguousarray(a, dtype=dtype)
     if arr.size == 0:
@@ -134,6 +143,31 @@ def pair_lists(nfa, first, limit: int = PAIR_LIMIT):
     return row.astype(np.int32), recs
 
 
+def lane_state_records(nfa) -> np.ndarray | None:
+    """Lane record (gbfsm_lane_rec) of every state, uint32[n, 4], or None when the
+    automaton has 2^26 states or more."""
+    n = int(nfa.num_states)
+    if n >= 1 << native.LANE_STATE_BITS:
+        return None
+    srp = np.asarray(nfa.sym_row_ptr, dtype=np.int64)
+    syms = np.asarray(nfa.sym_symbols, dtype=np.int64)
+    nnz = int(srp[-1])
+    deg = srp[1:] - srp[:-1]
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    has_any = np.bincount(src[syms == ANY_SYMBOL], minlength=n)[:n] > 0
+    slow = (deg > native.LANE_FAST_DEGREE) | has_any
+    j = np.arange(native.LANE_FAST_DEGREE, dtype=np.int64)
+    idx = np.minimum(srp[:-1, None] + j[None, :], max(nnz - 1, 0))
+    lab = np.where(j[None, :] < deg[:, None], syms[idx] if nnz else 0, 0) & 0xFF
+    lo = lab[:, 0] | (lab[:, 1] << 8) | (lab[:, 2] << 16) | (lab[:, 3] << 24)
+    hi = lab[:, 4] | (lab[:, 5] << 8) | (lab[:, 6] << 16) | (lab[:, 7] << 24)
+    acc = np.asarray(nfa.accept, dtype=bool)
+    x = (np.arange(n, dtype=np.int64) | (np.where(slow, 0, deg) << native.LANE_DEG_SHIFT)
+         | (slow.astype(np.int64) << 30) | (acc.astype(np.int64) << 31))
+    recs = np.stack([x, srp[:-1], np.where(slow, srp[1:], lo), np.where(slow, 0, hi)], axis=1)
+    return recs.astype(np.uint32)
+
+
 class DeviceNFA:
     """An NFA (ours or gpufsm's, duck-typed on the CSR fields) resident on a GPU."""
 
@@ -211,21 +245,26 @@ class DeviceNFA:
         self.lanes = pairs is not None
         self.pair_sizes = np.diff(pairs[0]).astype(np.int32) if pairs is not None else None
         self.pair_mean = float(self.pair_sizes.mean()) if pairs is not None else float("inf")
+        lane_states = lane_state_records(nfa) if pairs is not None else None
+        if lane_states is None:
+            pairs = None
+            self.lanes = False
+            self.pair_sizes, self.pair_mean = None, float("inf")
         if pairs is not None:
             prow, precs = pairs
+            tg = np.asarray(nfa.sym_targets, dtype=np.int64)
             with torch.cuda.device(dev):
                 self.edge_sym = _padded(max(1, nnz), 2, dev, torch.int16)
                 if nnz:
                     self.edge_sym[:nnz].copy_(torch.from_numpy(
                         np.ascontiguousarray(ssy, dtype=np.int16)))
                 self.pair_row = torch.from_numpy(np.ascontiguousarray(prow)).to(dev)
-                self.pair_edges = _padded(max(1, precs.shape[0]), 16, dev)
-                if precs.size:
-                    self.pair_edges[: precs.nbytes].copy_(
-                        torch.from_numpy(np.ascontiguousarray(precs).view(np.uint8).ravel()))
+                self.pair_lanes = _records(lane_states[precs[:, 0].astype(np.int64)], dev)
+                self.lane_edges = _records(lane_states[tg] if nnz else lane_states[:0], dev)
             d.edge_sym = self.edge_sym.data_ptr()
             d.pair_row = self.pair_row.data_ptr()
-            d.pair_edges = self.pair_edges.data_ptr()
+            d.pair_lanes = self.pair_lanes.data_ptr()
+            d.lane_edges = self.lane_edges.data_ptr()
         self.desc = d
 
     @property

@@ -57,8 +57,21 @@ class NfaDev(ctypes.Structure):
         ("first_edges", ctypes.c_void_p),
         ("edge_sym", ctypes.c_void_p),
         ("pair_row", ctypes.c_void_p),
-        ("pair_edges", ctypes.c_void_p),
+        ("pair_lanes", ctypes.c_void_p),
+        ("lane_edges", ctypes.c_void_p),
     ]
+
+
+class LaneRec(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_uint32), ("row_begin", ctypes.c_uint32),
+                ("labels_lo", ctypes.c_uint32), ("labels_hi", ctypes.c_uint32)]
+
+
+LANE_STATE_BITS = 26  # GBFSM_LANE_STATE_MASK
+LANE_DEG_SHIFT = 26
+LANE_SLOW = 1 << 30
+LANE_ACCEPT = 1 << 31
+LANE_FAST_DEGREE = 8  # most out-edges of a state in the packed-label form
 
 
 class DfaDev(ctypes.Structure):

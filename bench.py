@@ -24,7 +24,7 @@ Printed (rank 0, one JSON line):
   serving     the continuous-batching loop on the c5 trace (p50 / p99 latency, offered
               GB/s, against one plain launch per request);
   roofline    the dominant kernel (the lane launch) against the measured HBM copy
-              bandwidth, with an L2 view beside it;
+              bandwidth, with the input stream alone beside it;
   cpu_baseline the CPU oracle port on this host's cores on a bounded sample.
 
 With ``--impl reference`` the reference's CPU algorithm (the C port of
@@ -398,7 +398,6 @@ def main(argv=None) -> int:
             parts = line.split()
             if len(parts) == 3 and parts[0] == kernel_name and parts[1] == args.workload:
                 traffic = int(parts[2])
-    l2 = l2_copy_gbs(dev)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
@@ -406,9 +405,8 @@ def main(argv=None) -> int:
                 "algorithmic_bytes_per_launch": int(algo),
                 "input_stream": {"achieved": examined_bytes / (kernel_ms * 1e-3) / 1e9,
                                  "frac": examined_bytes / (kernel_ms * 1e-3) / 1e9 / hbm},
-                "l2": {"peak": l2, "frac": achieved / l2 if l2 else None,
-                       "peak_source": "measured here: L2-resident elementwise copy kernel, "
-                                      "2 x 24 MiB"}}
+                "note": "algorithmic bytes are mostly edge gathers served by L1/L2 (see "
+                        "profiles/lanes_kernel_c3-sustained.md); DRAM carries the input"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
@@ -433,29 +431,6 @@ def main(argv=None) -> int:
     if world > 1:
         dist.destroy_process_group()
     return 0
-
-
-def l2_copy_gbs(dev) -> float | None:
-    """Read+write GB/s of an L2-resident elementwise copy kernel (2 x 24 MiB, best of 20,
-    CUDA events)."""
-    import torch
-
-    try:
-        a = torch.ones(6 << 20, dtype=torch.int32, device=dev)
-        b = torch.empty_like(a)
-        best = float("inf")
-        for _ in range(20):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(10):
-                torch.mul(a, 1, out=b)
-            e1.record()
-            e1.synchronize()
-            best = min(best, e0.elapsed_time(e1) / 10)
-        return 2 * a.numel() * 4 / (best * 1e-3) / 1e9
-    except RuntimeError:
-        return None
 
 
 def serving_section(dev, n_requests: int, slo_ms: float) -> dict:

@@ -75,6 +75,23 @@ typedef struct gbfsm_edge {
 
 /* An NFA on the device (all pointers are device pointers). Built from the reference's
  * CSR arrays (src/gpufsm/core/nfa.py:56-65) by gbfsm_nfa_layout. */
+/* A state as a lane of the one-chunk-per-lane kernel holds it: the state, its accept
+ * flag and its out-edges in 16 bytes. When the state has at most 8 symbol edges and no
+ * ANY edge (the fast form) their symbols are packed one byte each into labels_lo
+ * (edges 0..3, lowest byte first) and labels_hi (edges 4..7), so a lane finds the
+ * edges matching a byte with two byte-wise compares. Otherwise (GBFSM_LANE_SLOW)
+ * labels_lo holds row_end and the lane scans edge_sym. */
+typedef struct gbfsm_lane_rec {
+    uint32_t state;     /* bits 0-25 state, 26-29 out-degree (fast form), 30 SLOW, 31 ACCEPT */
+    uint32_t row_begin;
+    uint32_t labels_lo;
+    uint32_t labels_hi;
+} gbfsm_lane_rec;
+#define GBFSM_LANE_STATE_MASK 0x03FFFFFFu
+#define GBFSM_LANE_DEG_SHIFT 26
+#define GBFSM_LANE_SLOW (1u << 30)
+#define GBFSM_LANE_ACCEPT (1u << 31)
+
 typedef struct gbfsm_nfa_dev {
     int32_t num_states;
     int32_t start_state;
@@ -94,14 +111,16 @@ typedef struct gbfsm_nfa_dev {
      * makes them a safe starting superset for a chunk that begins mid-input. */
     const uint32_t *first_row;
     const gbfsm_edge *first_edges;
-    /* Optional (NULL = no lane-per-chunk speculation): the label of every symbol edge as
-     * uint16 (0..256), read to filter a state's edges before loading their records; and,
-     * for automata without epsilon edges, the two-byte supersets: for bytes c1, c2 the
-     * distinct states reachable from any state by c1 then c2, as state records
-     * pair_edges[pair_row[c1*256 + c2] .. pair_row[c1*256 + c2 + 1]) (65537 entries). */
+    /* Optional (NULL = no lane-per-chunk speculation; automata without epsilon edges and
+     * with fewer than 2^26 states): the label of every symbol edge as uint16 (0..256);
+     * the two-byte supersets: for bytes c1, c2 the distinct states reachable from any
+     * state by c1 then c2, as lane records pair_lanes[pair_row[c1*256 + c2] ..
+     * pair_row[c1*256 + c2 + 1]) (65537 entries); and for every symbol edge the lane
+     * record of its target (lane_edges, indexed like sym_edges). */
     const uint16_t *edge_sym;
     const uint32_t *pair_row;
-    const gbfsm_edge *pair_edges;
+    const gbfsm_lane_rec *pair_lanes;
+    const gbfsm_lane_rec *lane_edges;
 } gbfsm_nfa_dev;
 
 /* A DFA on the device. table[s * 256 + c] holds the successor of s on byte c in the low

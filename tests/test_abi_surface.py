@@ -65,7 +65,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     pairs = {"gbfsm_edge": native.Edge, "gbfsm_nfa_dev": native.NfaDev,
              "gbfsm_dfa_dev": native.DfaDev, "gbfsm_plan": native.Plan,
              "gbfsm_automaton": native.Automaton, "gbfsm_task": native.Task,
-             "gbfsm_chunk": native.Chunk, "gbfsm_chunk_io": native.ChunkIO}
+             "gbfsm_chunk": native.Chunk, "gbfsm_chunk_io": native.ChunkIO,
+             "gbfsm_lane_rec": native.LaneRec}
     src = tmp_path / "probe.c"
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gbfsm.h"', "int main(void) {"]
     for name in pairs:

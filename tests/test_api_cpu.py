@@ -171,3 +171,32 @@ def test_batch_results_and_benchmark_stats_conventions():
     assert st.as_row()["backend"] == "cuda"
     with pytest.raises(ValueError):
         G.benchmark(_nfa(), b"a", repeats=0)
+
+
+def test_lane_state_records_pack_labels_degree_and_flags():
+    """gbfsm_lane_rec of each state: packed labels for <= 8 edges without ANY, else SLOW."""
+    from abstraction_regret_gb300 import native
+    from abstraction_regret_gb300.device import lane_state_records
+
+    b = G.NFABuilder()
+    for k in range(4):
+        b.add_state(accept=(k == 2))
+    b.set_start(0)
+    for sym in (5, 7, 255):          # state 0: three edges, fast form
+        b.add_transition(0, sym, 1)
+    for sym in range(9):             # state 1: nine edges, slow (degree above 8)
+        b.add_transition(1, sym, 2)
+    b.add_transition(2, G.ANY_SYMBOL, 3)  # state 2: ANY edge, slow
+    nfa = b.build()                  # state 3: no edges, fast with degree 0
+    recs = lane_state_records(nfa)
+    srp = np.asarray(nfa.sym_row_ptr)
+    x = recs[:, 0].astype(np.int64)
+    assert list(x & 0x3FFFFFF) == [0, 1, 2, 3]
+    assert list((x >> 30) & 1) == [0, 1, 1, 0]
+    assert list((x >> 31) & 1) == [0, 0, 1, 0]
+    assert (x[0] >> native.LANE_DEG_SHIFT) & 15 == 3 and (x[3] >> native.LANE_DEG_SHIFT) & 15 == 0
+    assert list(recs[:, 1]) == list(srp[:-1])
+    row0 = sorted(int(s) for s in np.asarray(nfa.sym_symbols)[srp[0]:srp[1]])
+    packed = [(int(recs[0, 2]) >> (8 * j)) & 0xFF for j in range(3)]
+    assert sorted(packed) == row0
+    assert recs[1, 2] == srp[2] and recs[2, 2] == srp[3]  # slow form: row_end
