@@ -294,27 +294,59 @@ __device__ __forceinline__ void add_match(uint32_t (&mk)[kLaneSlots], int &nm, u
     ++nm;
 }
 
+// Bit 7 of each byte of the result is set where the byte of x is zero (exact: the
+// per-byte sum cannot carry into the next byte).
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
+    const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+    return ~(t | x) & 0x80808080u;
+}
+
+// Markers (bit 7 of byte j) of the packed labels of a fast-form record equal to the byte,
+// limited to its first `deg` labels: edges 0..3 in lo, 4..7 in hi.
+__device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4, uint32_t &m_lo,
+                                              uint32_t &m_hi) {
+    const uint32_t deg = (r.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
+    m_lo = zero_bytes(r.z ^ sym4);
+    m_hi = zero_bytes(r.w ^ sym4);
+    m_lo &= deg >= 4u ? 0xFFFFFFFFu : (1u << (8u * deg)) - 1u;
+    m_hi &= deg >= 8u ? 0xFFFFFFFFu : deg <= 4u ? 0u : (1u << (8u * (deg - 4u))) - 1u;
+}
+
 // One byte: returns the new member count (acc: a member accepts), or -1 when more than
 // kLaneSlots edges match.
 __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
                                          uint32_t sym, const uint16_t *__restrict__ labels,
                                          const gbfsm_lane_rec *__restrict__ recs) {
+    const uint32_t sym4 = sym * 0x01010101u;
+    // the common case: one member in the fast form with at most one matching edge
+    if (valid == 1u && !(cur[0].x & GBFSM_LANE_SLOW)) {
+        uint32_t m_lo, m_hi;
+        label_matches(cur[0], sym4, m_lo, m_hi);
+        const int c = __popc(m_lo) + __popc(m_hi);
+        if (c == 0) {
+            valid = 0;
+            acc = false;
+            return 0;
+        }
+        if (c == 1) {
+            const uint32_t p = m_lo ? (uint32_t)(__ffs(m_lo) - 1) >> 3
+                                    : 4u + ((uint32_t)(__ffs(m_hi) - 1) >> 3);
+            cur[0] = ld_lane(recs + cur[0].y + p);
+            acc = (cur[0].x & GBFSM_LANE_ACCEPT) != 0u;
+            return 1;
+        }
+    }
     uint32_t mk[kLaneSlots];
     int nm = 0;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0;
-    const uint32_t sym4 = sym * 0x01010101u;
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) {
         if (!((valid >> q) & 1u)) continue;
         const uint4 r = cur[q];
         if (!(r.x & GBFSM_LANE_SLOW)) {
-            const uint32_t deg = (r.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
-            // byte-wise equality, limited to the first deg labels
-            uint32_t m_lo = __vcmpeq4(r.z, sym4) & 0x80808080u;
-            uint32_t m_hi = __vcmpeq4(r.w, sym4) & 0x80808080u;
-            m_lo &= deg >= 4u ? 0xFFFFFFFFu : (1u << (8u * deg)) - 1u;
-            m_hi &= deg >= 8u ? 0xFFFFFFFFu : deg <= 4u ? 0u : (1u << (8u * (deg - 4u))) - 1u;
+            uint32_t m_lo, m_hi;
+            label_matches(r, sym4, m_lo, m_hi);
             while (m_lo) {
                 add_match(mk, nm, r.y + ((uint32_t)(__ffs(m_lo) - 1) >> 3));
                 m_lo &= m_lo - 1u;
@@ -390,18 +422,22 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
     }
     const uint16_t *__restrict__ labels = A.edge_sym;
     const gbfsm_lane_rec *__restrict__ recs = A.lane_edges;
-    const int64_t len = e - b;
+    const int32_t len = (int32_t)(e - b);
+    const int32_t b32 = (int32_t)b;
     ByteStream bytes;
     bytes.init(base + b, stopped ? 0 : len);
-    int64_t j = 0;
+    int32_t j = 0;
     int m = __popc(valid);
-    while (!stopped && j < len) {
+    // the first kOverlap bytes: set sizes at the checkpoints; a later chunk's accept there
+    // is recorded without stopping
+    const int32_t head = min(len, (int32_t)kOverlap);
+    while (!stopped && j < head) {
         const uint32_t sym = bytes.next();
         ++j;
         bool acc;
         m = lane_step(cur, valid, acc, sym, labels, recs);
         if (m < 0) return false;
-        const int32_t pos = (int32_t)(b + j);
+        const int32_t pos = b32 + j;
         if (m == 0) {  // reference.py:59-60
             dead_at = pos;
             stopped = true;
@@ -414,12 +450,27 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
                 break;
             }
             note_accept(acc_after, j, pos);
-            if (j > kOverlap) stopped = true;
         }
         const int c = checkpoint_of(j);
 #pragma unroll
         for (int q = 0; q < kCheckpoints; ++q)
             if (q == c) counts[q] = m;
+    }
+    // the rest: no checkpoints, and any accept ends the run
+    while (!stopped && j < len) {
+        const uint32_t sym = bytes.next();
+        ++j;
+        bool acc;
+        m = lane_step(cur, valid, acc, sym, labels, recs);
+        if (m < 0) return false;
+        if (m == 0) {
+            dead_at = b32 + j;
+            stopped = true;
+        } else if (acc) {
+            if (index == 0) acc_after[0] = b32 + j;
+            else note_accept(acc_after, j, b32 + j);
+            stopped = true;
+        }
     }
 #pragma unroll
     for (int c = 0; c < kCheckpoints; ++c) {

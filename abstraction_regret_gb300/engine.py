@@ -213,15 +213,29 @@ class PersistentEngine:
         size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
         return int(min(size, 1 << 20))
 
-    def auto_lane_chunk_bytes(self, nfa_bytes: int) -> int:
-        """Lane chunks: about one per resident lane of the lane launch, so that the batch
-        runs in a single wave (the power of two nearest to bytes / lanes, in
-        [MIN_CHUNK, 1 MiB]). A lane's steps are dependent L2 round trips, so splitting
-        finer only adds chunk overhead once every lane is busy."""
-        lanes = self.sm_count * LANE_WARPS_PER_SM * 32
-        per = max(1.0, nfa_bytes / lanes)
-        size = 1 << int(round(np.log2(per)))
-        return int(min(max(size, MIN_CHUNK), 1 << 20))
+    def auto_lane_chunk_bytes(self, lengths: np.ndarray, aut: np.ndarray) -> int:
+        """Lane chunks: the smallest size (a multiple of 64 bytes, at least MIN_CHUNK)
+        whose LANES tasks (32 chunks each, per automaton) fit the lane launch's resident
+        warps, so the batch runs in one full wave. A lane's steps are dependent L2 round
+        trips: once every lane is busy, finer chunks only add per-chunk work, and a second
+        partial wave adds its whole duration."""
+        warps = self.sm_count * LANE_WARPS_PER_SM
+        lengths = np.asarray(lengths, dtype=np.int64)
+        aut = np.asarray(aut, dtype=np.int64)
+        if lengths.size == 0:
+            return MIN_CHUNK
+        total = int(lengths.sum())
+        size = max(MIN_CHUNK, -(-total // (warps * LANE_GROUP) // 64) * 64)
+        order = np.argsort(aut, kind="stable")
+        a_sorted, l_sorted = aut[order], lengths[order]
+        seg = np.flatnonzero(np.r_[True, a_sorted[1:] != a_sorted[:-1]])
+        while size < (1 << 20):
+            chunks = np.maximum(1, -(-l_sorted // size))
+            per_aut = np.add.reduceat(chunks, seg) if seg.size else np.zeros(0, np.int64)
+            if int((-(-per_aut // LANE_GROUP)).sum()) <= warps:
+                break
+            size += 64
+        return int(min(size, 1 << 20))
 
     def make_tasks(self, aut_ids, lengths, starts=None) -> TaskPlan:
         """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
@@ -258,7 +272,7 @@ class PersistentEngine:
                 chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
             else:
                 chunk_w = self.auto_chunk_bytes(int(lengths[warp_in].sum()))
-                chunk_l = self.auto_lane_chunk_bytes(int(lengths[lane_in].sum()))
+                chunk_l = self.auto_lane_chunk_bytes(lengths[lane_in], aut_ids[lane_in])
             csize[warp_in] = chunk_w
             csize[lane_in] = chunk_l
         # every input of a lane automaton is chunked (a short one is a single exact

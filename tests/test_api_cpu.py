@@ -200,3 +200,26 @@ def test_lane_state_records_pack_labels_degree_and_flags():
     packed = [(int(recs[0, 2]) >> (8 * j)) & 0xFF for j in range(3)]
     assert sorted(packed) == row0
     assert recs[1, 2] == srp[2] and recs[2, 2] == srp[3]  # slow form: row_end
+
+
+def test_lane_chunk_size_fills_one_wave():
+    """The auto lane chunk size is the smallest whose LANES tasks fit the resident warps."""
+    from types import SimpleNamespace
+
+    from abstraction_regret_gb300 import workloads as W
+    from abstraction_regret_gb300.engine import (LANE_GROUP, LANE_WARPS_PER_SM, MIN_CHUNK,
+                                                 PersistentEngine)
+
+    eng = SimpleNamespace(sm_count=152)
+    pick = PersistentEngine.auto_lane_chunk_bytes
+    assert pick(eng, np.zeros(0, np.int64), np.zeros(0, np.int64)) == MIN_CHUNK
+    assert pick(eng, np.full(8, 1000), np.zeros(8, np.int64)) == MIN_CHUNK
+    lengths = W.log_uniform_lengths(np.random.default_rng([2, 1]), 2048, 256, 1 << 20)
+    aut = np.zeros(lengths.size, np.int64)
+    size = pick(eng, lengths, aut)
+    warps = 152 * LANE_WARPS_PER_SM
+
+    def tasks(s):
+        return -(-int(np.maximum(1, -(-lengths // s)).sum()) // LANE_GROUP)
+
+    assert size % 64 == 0 and tasks(size) <= warps < tasks(size - 64)
