@@ -265,23 +265,26 @@ __device__ inline uint4 lane_record_of(const gbfsm_nfa_dev &A, uint32_t s) {
     const bool acc =
         (__ldg(reinterpret_cast<const unsigned long long *>(A.accept_words) + (s >> 6)) >>
          (s & 63u)) & 1ull;
-    bool slow = deg > 8u;
+    bool slow = deg > (uint32_t)GBFSM_LANE_FAST_DEGREE;
     uint32_t lo = 0, hi = 0;
     for (uint32_t j = 0; j < deg && !slow; ++j) {
         const uint32_t sym = __ldg(A.edge_sym + rb + j);
         if (sym == (uint32_t)GBFSM_ANY_SYMBOL) slow = true;
         if (j < 4) lo |= (sym & 0xFFu) << (8u * j);
-        else hi |= (sym & 0xFFu) << (8u * (j - 4));
+        else if (j < 8) hi |= (sym & 0xFFu) << (8u * (j - 4));
     }
     const uint32_t x = s | (slow ? 0u : deg << GBFSM_LANE_DEG_SHIFT) |
                        (slow ? GBFSM_LANE_SLOW : 0u) | (acc ? GBFSM_LANE_ACCEPT : 0u);
     return slow ? make_uint4(x, rb, re, 0u) : make_uint4(x, rb, lo, hi);
 }
 
+__device__ __forceinline__ uint32_t lane_degree(uint32_t x) {
+    return (x >> GBFSM_LANE_DEG_SHIFT) & GBFSM_LANE_DEG_MASK;
+}
+
 // The engine state record (as WarpNfa keeps it) of a lane record.
 __device__ __forceinline__ uint4 warp_record_of(uint4 l) {
-    const uint32_t deg = (l.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
-    const uint32_t re = (l.x & GBFSM_LANE_SLOW) ? l.z : l.y + deg;
+    const uint32_t re = (l.x & GBFSM_LANE_SLOW) ? l.z : l.y + lane_degree(l.x);
     return make_uint4(l.x & GBFSM_LANE_STATE_MASK,
                       (l.x & GBFSM_LANE_ACCEPT) ? GBFSM_EDGE_ACCEPT : 0u, l.y, re);
 }
@@ -301,37 +304,49 @@ __device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
     return ~(t | x) & 0x80808080u;
 }
 
-// Markers (bit 7 of byte j) of the packed labels of a fast-form record equal to the byte,
-// limited to its first `deg` labels: edges 0..3 in lo, 4..7 in hi.
-__device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4, uint32_t &m_lo,
-                                              uint32_t &m_hi) {
-    const uint32_t deg = (r.x >> GBFSM_LANE_DEG_SHIFT) & 15u;
-    m_lo = zero_bytes(r.z ^ sym4);
-    m_hi = zero_bytes(r.w ^ sym4);
-    m_lo &= deg >= 4u ? 0xFFFFFFFFu : (1u << (8u * deg)) - 1u;
-    m_hi &= deg >= 8u ? 0xFFFFFFFFu : deg <= 4u ? 0u : (1u << (8u * (deg - 4u))) - 1u;
+// Byte markers of the first k (< 0: none, >= 4: all four) bytes of a word.
+__device__ __forceinline__ uint32_t first_bytes(int k) {
+    return k >= 4 ? 0x80808080u : k <= 0 ? 0u : 0x80808080u & ((1u << (8 * k)) - 1u);
+}
+
+// Markers (bit 7 of byte j of word w: edge 4w + j) of the labels of a fast-form record
+// equal to the byte: edges 0..7 from the record, edges 8..15 from the ext table.
+__device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4,
+                                              const uint2 *__restrict__ ext,
+                                              uint32_t (&m)[4]) {
+    const int deg = (int)lane_degree(r.x);
+    m[0] = zero_bytes(r.z ^ sym4) & first_bytes(deg);
+    m[1] = zero_bytes(r.w ^ sym4) & first_bytes(deg - 4);
+    m[2] = 0u;
+    m[3] = 0u;
+    if (deg > 8) {
+        const uint2 h = __ldg(ext + (r.x & GBFSM_LANE_STATE_MASK));
+        m[2] = zero_bytes(h.x ^ sym4) & first_bytes(deg - 8);
+        m[3] = zero_bytes(h.y ^ sym4) & first_bytes(deg - 12);
+    }
 }
 
 // One byte: returns the new member count (acc: a member accepts), or -1 when more than
 // kLaneSlots edges match.
 __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
                                          uint32_t sym, const uint16_t *__restrict__ labels,
-                                         const gbfsm_lane_rec *__restrict__ recs) {
+                                         const gbfsm_lane_rec *__restrict__ recs,
+                                         const uint2 *__restrict__ ext) {
     const uint32_t sym4 = sym * 0x01010101u;
     // the common case: one member in the fast form with at most one matching edge
     if (valid == 1u && !(cur[0].x & GBFSM_LANE_SLOW)) {
-        uint32_t m_lo, m_hi;
-        label_matches(cur[0], sym4, m_lo, m_hi);
-        const int c = __popc(m_lo) + __popc(m_hi);
+        uint32_t m[4];
+        label_matches(cur[0], sym4, ext, m);
+        const int c = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
         if (c == 0) {
             valid = 0;
             acc = false;
             return 0;
         }
         if (c == 1) {
-            const uint32_t p = m_lo ? (uint32_t)(__ffs(m_lo) - 1) >> 3
-                                    : 4u + ((uint32_t)(__ffs(m_hi) - 1) >> 3);
-            cur[0] = ld_lane(recs + cur[0].y + p);
+            const uint32_t w = m[0] ? m[0] : m[1] ? m[1] : m[2] ? m[2] : m[3];
+            const uint32_t base = m[0] ? 0u : m[1] ? 4u : m[2] ? 8u : 12u;
+            cur[0] = ld_lane(recs + cur[0].y + base + ((uint32_t)(__ffs(w) - 1) >> 3));
             acc = (cur[0].x & GBFSM_LANE_ACCEPT) != 0u;
             return 1;
         }
@@ -345,15 +360,14 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
         if (!((valid >> q) & 1u)) continue;
         const uint4 r = cur[q];
         if (!(r.x & GBFSM_LANE_SLOW)) {
-            uint32_t m_lo, m_hi;
-            label_matches(r, sym4, m_lo, m_hi);
-            while (m_lo) {
-                add_match(mk, nm, r.y + ((uint32_t)(__ffs(m_lo) - 1) >> 3));
-                m_lo &= m_lo - 1u;
-            }
-            while (m_hi) {
-                add_match(mk, nm, r.y + 4u + ((uint32_t)(__ffs(m_hi) - 1) >> 3));
-                m_hi &= m_hi - 1u;
+            uint32_t m[4];
+            label_matches(r, sym4, ext, m);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                while (m[w]) {
+                    add_match(mk, nm, r.y + 4u * w + ((uint32_t)(__ffs(m[w]) - 1) >> 3));
+                    m[w] &= m[w] - 1u;
+                }
             }
         } else {
             for (uint32_t k = r.y; k < r.z; ++k) {
@@ -422,6 +436,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
     }
     const uint16_t *__restrict__ labels = A.edge_sym;
     const gbfsm_lane_rec *__restrict__ recs = A.lane_edges;
+    const uint2 *__restrict__ ext = reinterpret_cast<const uint2 *>(A.lane_labels_ext);
     const int32_t len = (int32_t)(e - b);
     const int32_t b32 = (int32_t)b;
     ByteStream bytes;
@@ -435,7 +450,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         const uint32_t sym = bytes.next();
         ++j;
         bool acc;
-        m = lane_step(cur, valid, acc, sym, labels, recs);
+        m = lane_step(cur, valid, acc, sym, labels, recs, ext);
         if (m < 0) return false;
         const int32_t pos = b32 + j;
         if (m == 0) {  // reference.py:59-60
@@ -461,7 +476,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         const uint32_t sym = bytes.next();
         ++j;
         bool acc;
-        m = lane_step(cur, valid, acc, sym, labels, recs);
+        m = lane_step(cur, valid, acc, sym, labels, recs, ext);
         if (m < 0) return false;
         if (m == 0) {
             dead_at = b32 + j;
@@ -495,7 +510,7 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         }
         for (int64_t t = 1; t <= ov_end - e; ++t) {
             bool acc;
-            const int nm = lane_step(cur, valid, acc, byte_at(base + e + t - 1), labels, recs);
+            const int nm = lane_step(cur, valid, acc, byte_at(base + e + t - 1), labels, recs, ext);
             if (nm < 0) break;
             ov_len = (int32_t)t;
             if (nm == 0) {

@@ -143,9 +143,9 @@ def pair_lists(nfa, first, limit: int = PAIR_LIMIT):
     return row.astype(np.int32), recs
 
 
-def lane_state_records(nfa) -> np.ndarray | None:
-    """Lane record (gbfsm_lane_rec) of every state, uint32[n, 4], or None when the
-    automaton has 2^26 states or more."""
+def lane_state_records(nfa):
+    """Lane record (gbfsm_lane_rec) of every state, uint32[n, 4], and the packed symbols
+    of its edges 8..15, uint32[n, 2]; None when the automaton has 2^25 states or more."""
     n = int(nfa.num_states)
     if n >= 1 << native.LANE_STATE_BITS:
         return None
@@ -159,13 +159,15 @@ def lane_state_records(nfa) -> np.ndarray | None:
     j = np.arange(native.LANE_FAST_DEGREE, dtype=np.int64)
     idx = np.minimum(srp[:-1, None] + j[None, :], max(nnz - 1, 0))
     lab = np.where(j[None, :] < deg[:, None], syms[idx] if nnz else 0, 0) & 0xFF
-    lo = lab[:, 0] | (lab[:, 1] << 8) | (lab[:, 2] << 16) | (lab[:, 3] << 24)
-    hi = lab[:, 4] | (lab[:, 5] << 8) | (lab[:, 6] << 16) | (lab[:, 7] << 24)
+    words = [lab[:, 4 * k] | (lab[:, 4 * k + 1] << 8) | (lab[:, 4 * k + 2] << 16)
+             | (lab[:, 4 * k + 3] << 24) for k in range(4)]
+    lo, hi = words[0], words[1]
+    ext = np.stack([np.where(slow, 0, words[2]), np.where(slow, 0, words[3])], axis=1)
     acc = np.asarray(nfa.accept, dtype=bool)
     x = (np.arange(n, dtype=np.int64) | (np.where(slow, 0, deg) << native.LANE_DEG_SHIFT)
          | (slow.astype(np.int64) << 30) | (acc.astype(np.int64) << 31))
     recs = np.stack([x, srp[:-1], np.where(slow, srp[1:], lo), np.where(slow, 0, hi)], axis=1)
-    return recs.astype(np.uint32)
+    return recs.astype(np.uint32), ext.astype(np.uint32)
 
 
 class DeviceNFA:
@@ -245,8 +247,8 @@ class DeviceNFA:
         self.lanes = pairs is not None
         self.pair_sizes = np.diff(pairs[0]).astype(np.int32) if pairs is not None else None
         self.pair_mean = float(self.pair_sizes.mean()) if pairs is not None else float("inf")
-        lane_states = lane_state_records(nfa) if pairs is not None else None
-        if lane_states is None:
+        lane = lane_state_records(nfa) if pairs is not None else None
+        if lane is None:
             pairs = None
             self.lanes = False
             self.pair_sizes, self.pair_mean = None, float("inf")
@@ -259,12 +261,16 @@ class DeviceNFA:
                     self.edge_sym[:nnz].copy_(torch.from_numpy(
                         np.ascontiguousarray(ssy, dtype=np.int16)))
                 self.pair_row = torch.from_numpy(np.ascontiguousarray(prow)).to(dev)
+                lane_states, lane_ext = lane
                 self.pair_lanes = _records(lane_states[precs[:, 0].astype(np.int64)], dev)
                 self.lane_edges = _records(lane_states[tg] if nnz else lane_states[:0], dev)
+                self.lane_labels_ext = torch.from_numpy(
+                    np.ascontiguousarray(lane_ext).view(np.int32).ravel()).to(dev)
             d.edge_sym = self.edge_sym.data_ptr()
             d.pair_row = self.pair_row.data_ptr()
             d.pair_lanes = self.pair_lanes.data_ptr()
             d.lane_edges = self.lane_edges.data_ptr()
+            d.lane_labels_ext = self.lane_labels_ext.data_ptr()
         self.desc = d
 
     @property

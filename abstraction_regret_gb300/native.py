@@ -59,6 +59,7 @@ class NfaDev(ctypes.Structure):
         ("pair_row", ctypes.c_void_p),
         ("pair_lanes", ctypes.c_void_p),
         ("lane_edges", ctypes.c_void_p),
+        ("lane_labels_ext", ctypes.c_void_p),
     ]
 
 
@@ -67,11 +68,11 @@ class LaneRec(ctypes.Structure):
                 ("labels_lo", ctypes.c_uint32), ("labels_hi", ctypes.c_uint32)]
 
 
-LANE_STATE_BITS = 26  # GBFSM_LANE_STATE_MASK
-LANE_DEG_SHIFT = 26
+LANE_STATE_BITS = 25  # GBFSM_LANE_STATE_MASK
+LANE_DEG_SHIFT = 25
 LANE_SLOW = 1 << 30
 LANE_ACCEPT = 1 << 31
-LANE_FAST_DEGREE = 8  # most out-edges of a state in the packed-label form
+LANE_FAST_DEGREE = 16  # most out-edges of a state in the packed-label form
 
 
 class DfaDev(ctypes.Structure):

@@ -76,19 +76,22 @@ typedef struct gbfsm_edge {
 /* An NFA on the device (all pointers are device pointers). Built from the reference's
  * CSR arrays (src/gpufsm/core/nfa.py:56-65) by gbfsm_nfa_layout. */
 /* A state as a lane of the one-chunk-per-lane kernel holds it: the state, its accept
- * flag and its out-edges in 16 bytes. When the state has at most 8 symbol edges and no
- * ANY edge (the fast form) their symbols are packed one byte each into labels_lo
- * (edges 0..3, lowest byte first) and labels_hi (edges 4..7), so a lane finds the
- * edges matching a byte with two byte-wise compares. Otherwise (GBFSM_LANE_SLOW)
- * labels_lo holds row_end and the lane scans edge_sym. */
+ * flag and its out-edges in 16 bytes. When the state has at most 16 symbol edges and no
+ * ANY edge (the fast form) the symbols of its first 8 edges are packed one byte each
+ * into labels_lo (edges 0..3, lowest byte first) and labels_hi (edges 4..7), and those
+ * of edges 8..15 into lane_labels_ext[2*state], [2*state + 1]; a lane finds the edges
+ * matching a byte with byte-wise compares. Otherwise (GBFSM_LANE_SLOW) labels_lo holds
+ * row_end and the lane scans edge_sym. */
 typedef struct gbfsm_lane_rec {
-    uint32_t state;     /* bits 0-25 state, 26-29 out-degree (fast form), 30 SLOW, 31 ACCEPT */
+    uint32_t state;     /* bits 0-24 state, 25-29 out-degree (fast form), 30 SLOW, 31 ACCEPT */
     uint32_t row_begin;
     uint32_t labels_lo;
     uint32_t labels_hi;
 } gbfsm_lane_rec;
-#define GBFSM_LANE_STATE_MASK 0x03FFFFFFu
-#define GBFSM_LANE_DEG_SHIFT 26
+#define GBFSM_LANE_STATE_MASK 0x01FFFFFFu
+#define GBFSM_LANE_DEG_SHIFT 25
+#define GBFSM_LANE_DEG_MASK 31u
+#define GBFSM_LANE_FAST_DEGREE 16
 #define GBFSM_LANE_SLOW (1u << 30)
 #define GBFSM_LANE_ACCEPT (1u << 31)
 
@@ -115,12 +118,14 @@ typedef struct gbfsm_nfa_dev {
      * with fewer than 2^26 states): the label of every symbol edge as uint16 (0..256);
      * the two-byte supersets: for bytes c1, c2 the distinct states reachable from any
      * state by c1 then c2, as lane records pair_lanes[pair_row[c1*256 + c2] ..
-     * pair_row[c1*256 + c2 + 1]) (65537 entries); and for every symbol edge the lane
-     * record of its target (lane_edges, indexed like sym_edges). */
+     * pair_row[c1*256 + c2 + 1]) (65537 entries); for every symbol edge the lane
+     * record of its target (lane_edges, indexed like sym_edges); and the packed symbols
+     * of edges 8..15 of every state (lane_labels_ext, [2 * num_states]). */
     const uint16_t *edge_sym;
     const uint32_t *pair_row;
     const gbfsm_lane_rec *pair_lanes;
     const gbfsm_lane_rec *lane_edges;
+    const uint32_t *lane_labels_ext;
 } gbfsm_nfa_dev;
 
 /* A DFA on the device. table[s * 256 + c] holds the successor of s on byte c in the low

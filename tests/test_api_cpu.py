@@ -174,7 +174,7 @@ def test_batch_results_and_benchmark_stats_conventions():
 
 
 def test_lane_state_records_pack_labels_degree_and_flags():
-    """gbfsm_lane_rec of each state: packed labels for <= 8 edges without ANY, else SLOW."""
+    """gbfsm_lane_rec of each state: packed labels for <= 16 edges without ANY, else SLOW."""
     from abstraction_regret_gb300 import native
     from abstraction_regret_gb300.device import lane_state_records
 
@@ -184,17 +184,17 @@ def test_lane_state_records_pack_labels_degree_and_flags():
     b.set_start(0)
     for sym in (5, 7, 255):          # state 0: three edges, fast form
         b.add_transition(0, sym, 1)
-    for sym in range(9):             # state 1: nine edges, slow (degree above 8)
+    for sym in range(17):            # state 1: seventeen edges, slow (degree above 16)
         b.add_transition(1, sym, 2)
     b.add_transition(2, G.ANY_SYMBOL, 3)  # state 2: ANY edge, slow
     nfa = b.build()                  # state 3: no edges, fast with degree 0
-    recs = lane_state_records(nfa)
+    recs, ext = lane_state_records(nfa)
     srp = np.asarray(nfa.sym_row_ptr)
     x = recs[:, 0].astype(np.int64)
-    assert list(x & 0x3FFFFFF) == [0, 1, 2, 3]
+    assert list(x & 0x1FFFFFF) == [0, 1, 2, 3]
     assert list((x >> 30) & 1) == [0, 1, 1, 0]
     assert list((x >> 31) & 1) == [0, 0, 1, 0]
-    assert (x[0] >> native.LANE_DEG_SHIFT) & 15 == 3 and (x[3] >> native.LANE_DEG_SHIFT) & 15 == 0
+    assert (x[0] >> native.LANE_DEG_SHIFT) & 31 == 3 and (x[3] >> native.LANE_DEG_SHIFT) & 31 == 0
     assert list(recs[:, 1]) == list(srp[:-1])
     row0 = sorted(int(s) for s in np.asarray(nfa.sym_symbols)[srp[0]:srp[1]])
     packed = [(int(recs[0, 2]) >> (8 * j)) & 0xFF for j in range(3)]
@@ -223,3 +223,25 @@ def test_lane_chunk_size_fills_one_wave():
         return -(-int(np.maximum(1, -(-lengths // s)).sum()) // LANE_GROUP)
 
     assert size % 64 == 0 and tasks(size) <= warps < tasks(size - 64)
+
+
+def test_lane_records_pack_edges_8_to_15_separately():
+    from abstraction_regret_gb300 import native
+    from abstraction_regret_gb300.device import lane_state_records
+
+    b = G.NFABuilder()
+    b.add_state()
+    b.add_state()
+    b.set_start(0)
+    labels = [10 + k for k in range(12)]
+    for sym in labels:
+        b.add_transition(0, sym, 1)
+    nfa = b.build()
+    recs, ext = lane_state_records(nfa)
+    srp = np.asarray(nfa.sym_row_ptr)
+    got = np.asarray(nfa.sym_symbols)[srp[0]:srp[1]]
+    assert (int(recs[0, 0]) >> native.LANE_DEG_SHIFT) & 31 == 12
+    assert not (int(recs[0, 0]) >> 30) & 1
+    words = [int(recs[0, 2]), int(recs[0, 3]), int(ext[0, 0]), int(ext[0, 1])]
+    packed = [(words[k // 4] >> (8 * (k % 4))) & 0xFF for k in range(12)]
+    assert packed == [int(s) for s in got]
