@@ -351,6 +351,43 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
             return 1;
         }
     }
+    // the next most common: at most two members, each in the fast form with at most 8
+    // edges, and at most two matching edges between them
+    const bool v0 = valid & 1u, v1 = (valid >> 1) & 1u;
+    const bool small0 = !v0 || (!(cur[0].x & GBFSM_LANE_SLOW) && lane_degree(cur[0].x) <= 8u);
+    const bool small1 = !v1 || (!(cur[1].x & GBFSM_LANE_SLOW) && lane_degree(cur[1].x) <= 8u);
+    if ((valid & ~3u) == 0u && small0 && small1) {
+        const int d0 = v0 ? (int)lane_degree(cur[0].x) : 0;
+        const int d1 = v1 ? (int)lane_degree(cur[1].x) : 0;
+        uint32_t a0 = zero_bytes(cur[0].z ^ sym4) & first_bytes(d0);
+        uint32_t a1 = zero_bytes(cur[0].w ^ sym4) & first_bytes(d0 - 4);
+        uint32_t a2 = zero_bytes(cur[1].z ^ sym4) & first_bytes(d1);
+        uint32_t a3 = zero_bytes(cur[1].w ^ sym4) & first_bytes(d1 - 4);
+        const int c = __popc(a0) + __popc(a1) + __popc(a2) + __popc(a3);
+        if (c <= 2) {
+            const uint32_t rb0 = cur[0].y, rb1 = cur[1].y;
+            uint32_t e[2];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {  // the lowest remaining match, then clear it
+                const bool z0 = a0 != 0u, z1 = a1 != 0u, z2 = a2 != 0u;
+                const uint32_t w = z0 ? a0 : z1 ? a1 : z2 ? a2 : a3;
+                e[t] = (z0 ? rb0 : z1 ? rb0 + 4u : z2 ? rb1 : rb1 + 4u) +
+                       ((uint32_t)(__ffs(w) - 1) >> 3);
+                const uint32_t rest = w & (w - 1u);
+                if (z0) a0 = rest;
+                else if (z1) a1 = rest;
+                else if (z2) a2 = rest;
+                else a3 = rest;
+            }
+            if (c >= 1) cur[0] = ld_lane(recs + e[0]);
+            if (c == 2) cur[1] = ld_lane(recs + e[1]);
+            const bool two = c == 2 && ((cur[0].x ^ cur[1].x) & GBFSM_LANE_STATE_MASK) != 0u;
+            valid = c == 0 ? 0u : two ? 3u : 1u;
+            acc = (c >= 1 && (cur[0].x & GBFSM_LANE_ACCEPT)) ||
+                  (two && (cur[1].x & GBFSM_LANE_ACCEPT));
+            return c == 0 ? 0 : two ? 2 : 1;
+        }
+    }
     uint32_t mk[kLaneSlots];
     int nm = 0;
 #pragma unroll
