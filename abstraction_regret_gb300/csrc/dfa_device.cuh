@@ -35,19 +35,25 @@ struct RowIndex<uint16_t> {
     using type = uint32_t;
 };
 
+// Table entry lookup from one array: shared memory of this CTA (kStaged) or global
+// memory read through L2.
 template <typename Entry, bool kStaged>
-__device__ __forceinline__ uint32_t table_at(const Entry *t, uint32_t state, uint32_t byte) {
-    const typename RowIndex<Entry>::type idx =
-        (typename RowIndex<Entry>::type)state * (uint32_t)kAlphabet + byte;
-    if (kStaged) return t[idx];
-    return __ldg(t + idx);
-}
+struct ArrayTable {
+    const Entry *t;
+    __device__ __forceinline__ uint32_t operator()(uint32_t state, uint32_t byte) const {
+        const typename RowIndex<Entry>::type idx =
+            (typename RowIndex<Entry>::type)state * (uint32_t)kAlphabet + byte;
+        if (kStaged) return t[idx];
+        return __ldg(t + idx);
+    }
+};
 
-// One input, one thread. Returns (flag, len, examined) through references.
-template <typename Entry, bool kStaged>
-__device__ __forceinline__ void dfa_walk(const Entry *table, const uint32_t *accept_bits,
-                                         uint32_t start, const uint8_t *in, int64_t len,
-                                         int32_t &flag, int32_t &mlen, int64_t &examined) {
+// One input, one thread, table entries through `lookup(state, byte)`. Returns (flag,
+// len, examined) through references.
+template <typename Entry, typename Lookup>
+__device__ __forceinline__ void dfa_walk_with(const Lookup &table_at, const uint32_t *accept_bits,
+                                              uint32_t start, const uint8_t *in, int64_t len,
+                                              int32_t &flag, int32_t &mlen, int64_t &examined) {
     constexpr uint32_t ACC = EntryTraits<Entry>::kAccept;
     flag = 0;
     mlen = 0;
@@ -74,8 +80,7 @@ __device__ __forceinline__ void dfa_walk(const Entry *table, const uint32_t *acc
             const uint32_t w[4] = {cur4.x, cur4.y, cur4.z, cur4.w};
 #pragma unroll
             for (int b = 0; b < 16; ++b) {
-                const uint32_t e =
-                    table_at<Entry, kStaged>(table, cur, (w[b >> 2] >> ((b & 3) * 8)) & 0xffu);
+                const uint32_t e = table_at(cur, (w[b >> 2] >> ((b & 3) * 8)) & 0xffu);
                 cur = e & ~ACC;
                 if (e & ACC) {
                     flag = 1;
@@ -87,7 +92,7 @@ __device__ __forceinline__ void dfa_walk(const Entry *table, const uint32_t *acc
         } else {
             const int hi = remain < 16 ? (int)remain : 16;
             for (int b = k; b < hi; ++b) {
-                const uint32_t e = table_at<Entry, kStaged>(table, cur, byte_of(cur4, b));
+                const uint32_t e = table_at(cur, byte_of(cur4, b));
                 cur = e & ~ACC;
                 if (e & ACC) {
                     flag = 1;
@@ -104,6 +109,14 @@ __device__ __forceinline__ void dfa_walk(const Entry *table, const uint32_t *acc
         cur4 = nxt4;
         if (blk + 16 < end) nxt4 = ld_stream16(blk + 16);
     }
+}
+
+template <typename Entry, bool kStaged>
+__device__ __forceinline__ void dfa_walk(const Entry *table, const uint32_t *accept_bits,
+                                         uint32_t start, const uint8_t *in, int64_t len,
+                                         int32_t &flag, int32_t &mlen, int64_t &examined) {
+    dfa_walk_with<Entry>(ArrayTable<Entry, kStaged>{table}, accept_bits, start, in, len, flag,
+                         mlen, examined);
 }
 
 }  // namespace gbfsm

@@ -318,3 +318,33 @@ def test_lane_chunks_that_outgrow_the_lane_fall_back_to_warps():
     assert int(eng._tasks.d_overflow_count[0].item()) > 0
     of, ol, oe, _ = O.nfa_batch(nfa, data, off)
     assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
+
+
+@pytest.mark.parametrize("states", [257, 300, 1000, 2049, 4096])
+def test_dfa_table_split_over_a_cluster(states):
+    """2-byte tables of 257..4096 states are split by rows over 2..16 CTAs of a cluster
+    (distributed shared memory); verdicts equal the oracle's and the L2 path's."""
+    from abstraction_regret_gb300 import native
+    from abstraction_regret_gb300.executors import CudaDFAExecutor
+
+    rng = np.random.default_rng(states)
+    for p in (0.0, 0.002):
+        dfa = G.random_dfa(states, accept_prob=p, seed=states)
+        lengths = [0, 1, 15, 16, 17, 100, 1000, 5000] + list(rng.integers(1, 20000, 300))
+        inputs = [rng.integers(0, 256, int(k), dtype=np.uint8).tobytes() for k in lengths]
+        want = [O.simulate_dfa(dfa, x) for x in inputs]
+        staged = CudaDFAExecutor(dfa, plan=native.make_plan(native.TECH_DFA_WALK, stage=1))
+        through_l2 = CudaDFAExecutor(dfa, plan=native.make_plan(native.TECH_DFA_WALK, stage=0))
+        f, l, ex, _, _ = staged.run_arrays(inputs, with_examined=True)
+        assert list(zip(f.astype(bool).tolist(), l.tolist())) == want
+        f2, l2, ex2, _, _ = through_l2.run_arrays(inputs, with_examined=True)
+        assert np.array_equal(f, f2) and np.array_equal(l, l2) and np.array_equal(ex, ex2)
+    start_acc = G.DFABuilder()
+    for k in range(600):
+        start_acc.add_state(accept=(k == 0))
+    for s in range(600):
+        for c in range(256):
+            start_acc.add_transition(s, c, (s * 7 + c) % 600)
+    a = start_acc.build()
+    f, l, _, _, _ = CudaDFAExecutor(a).run_arrays([b"", b"xyz"])
+    assert f.tolist() == [1, 1] and l.tolist() == [0, 0]
