@@ -326,6 +326,30 @@ __device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4,
     }
 }
 
+// The set becomes the distinct targets of the matched edges mk[0 .. nm) (nm <= kLaneSlots),
+// their records loaded together; returns the member count (acc: a member accepts).
+__device__ __forceinline__ int load_targets(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
+                                            const uint32_t (&mk)[kLaneSlots], int nm,
+                                            const gbfsm_lane_rec *__restrict__ recs) {
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q)
+        cur[q] = (q < nm) ? ld_lane(recs + mk[q]) : make_uint4(0, 0, 0, 0);
+    valid = 0;
+    acc = false;
+#pragma unroll
+    for (int q = 0; q < kLaneSlots; ++q) {
+        bool keep = q < nm;
+#pragma unroll
+        for (int u = 0; u < q; ++u)
+            keep = keep && ((cur[u].x ^ cur[q].x) & GBFSM_LANE_STATE_MASK) != 0u;
+        if (keep) {
+            valid |= 1u << q;
+            acc |= (cur[q].x & GBFSM_LANE_ACCEPT) != 0u;
+        }
+    }
+    return __popc(valid);
+}
+
 // One byte: returns the new member count (acc: a member accepts), or -1 when more than
 // kLaneSlots edges match.
 __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
@@ -414,23 +438,56 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
         }
     }
     if (nm > kLaneSlots) return -1;
+    return load_targets(cur, valid, acc, mk, nm, recs);
+}
+
+// Start set of a later chunk at b when the two-byte superset there is too large for a
+// lane: the two-byte superset at b-2 (at most kWideStart members, streamed from
+// pair_lanes) stepped over x[b-2], then x[b-1] -- again a superset of the true set at
+// b, and usually far smaller. Returns false when the wide set is too large or a step
+// matches more than kLaneSlots edges.
+constexpr uint32_t kWideStart = 64;
+
+__device__ inline bool widened_start(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b,
+                                     const uint16_t *__restrict__ labels,
+                                     const gbfsm_lane_rec *__restrict__ recs,
+                                     const uint2 *__restrict__ ext, uint4 (&cur)[kLaneSlots],
+                                     uint32_t &valid) {
+    if (b < 4) return false;
+    const uint32_t key = byte_at(base + b - 4) * 256u + byte_at(base + b - 3);
+    const uint32_t pr = __ldg(A.pair_row + key);
+    const uint32_t cnt = __ldg(A.pair_row + key + 1) - pr;
+    if (cnt > kWideStart) return false;
+    const uint32_t sym = byte_at(base + b - 2);
+    const uint32_t sym4 = sym * 0x01010101u;
+    uint32_t mk[kLaneSlots];
+    int nm = 0;
 #pragma unroll
-    for (int q = 0; q < kLaneSlots; ++q)
-        cur[q] = (q < nm) ? ld_lane(recs + mk[q]) : make_uint4(0, 0, 0, 0);
-    valid = 0;
-    acc = false;
+    for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0;
+    for (uint32_t q = 0; q < cnt && nm <= kLaneSlots; ++q) {
+        const uint4 r = ld_lane(A.pair_lanes + pr + q);
+        if (!(r.x & GBFSM_LANE_SLOW)) {
+            uint32_t m[4];
+            label_matches(r, sym4, ext, m);
 #pragma unroll
-    for (int q = 0; q < kLaneSlots; ++q) {
-        bool keep = q < nm;
-#pragma unroll
-        for (int u = 0; u < q; ++u)
-            keep = keep && ((cur[u].x ^ cur[q].x) & GBFSM_LANE_STATE_MASK) != 0u;
-        if (keep) {
-            valid |= 1u << q;
-            acc |= (cur[q].x & GBFSM_LANE_ACCEPT) != 0u;
+            for (int w = 0; w < 4; ++w) {
+                while (m[w]) {
+                    add_match(mk, nm, r.y + 4u * w + ((uint32_t)(__ffs(m[w]) - 1) >> 3));
+                    m[w] &= m[w] - 1u;
+                }
+            }
+        } else {
+            for (uint32_t k = r.y; k < r.z; ++k) {
+                const uint32_t es = __ldg(labels + k);
+                if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) add_match(mk, nm, k);
+            }
         }
     }
-    return __popc(valid);
+    if (nm > kLaneSlots) return false;
+    bool acc;
+    load_targets(cur, valid, acc, mk, nm, recs);
+    if (valid == 0u) return true;
+    return lane_step(cur, valid, acc, byte_at(base + b - 1), labels, recs, ext) >= 0;
 }
 
 // Returns false, writing nothing, when a start superset or a byte's matches exceed
@@ -438,6 +495,9 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
 // ends the overlap run.
 __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b,
                                   int64_t e, int64_t ov_end, int index, ChunkRecord *rec) {
+    const uint16_t *__restrict__ labels = A.edge_sym;
+    const gbfsm_lane_rec *__restrict__ recs = A.lane_edges;
+    const uint2 *__restrict__ ext = reinterpret_cast<const uint2 *>(A.lane_labels_ext);
     uint4 cur[kLaneSlots];
 #pragma unroll
     for (int q = 0; q < kLaneSlots; ++q) cur[q] = make_uint4(0, 0, 0, 0);
@@ -461,19 +521,19 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         const uint32_t key = byte_at(base + b - 2) * 256u + byte_at(base + b - 1);
         const uint32_t pr = __ldg(A.pair_row + key);
         const uint32_t cnt = __ldg(A.pair_row + key + 1) - pr;
-        if (cnt > (uint32_t)kLaneSlots) return false;
+        if (cnt <= (uint32_t)kLaneSlots) {
 #pragma unroll
-        for (int q = 0; q < kLaneSlots; ++q)
-            if ((uint32_t)q < cnt) cur[q] = ld_lane(A.pair_lanes + pr + q);
-        valid = (1u << cnt) - 1u;
-        if (cnt == 0) {
+            for (int q = 0; q < kLaneSlots; ++q)
+                if ((uint32_t)q < cnt) cur[q] = ld_lane(A.pair_lanes + pr + q);
+            valid = (1u << cnt) - 1u;
+        } else if (!widened_start(A, base, b, labels, recs, ext, cur, valid)) {
+            return false;
+        }
+        if (valid == 0u) {
             dead_at = (int32_t)b;
             stopped = true;
         }
     }
-    const uint16_t *__restrict__ labels = A.edge_sym;
-    const gbfsm_lane_rec *__restrict__ recs = A.lane_edges;
-    const uint2 *__restrict__ ext = reinterpret_cast<const uint2 *>(A.lane_labels_ext);
     const int32_t len = (int32_t)(e - b);
     const int32_t b32 = (int32_t)b;
     ByteStream bytes;

@@ -47,8 +47,10 @@ NFA_BYTE_WEIGHT = 4  # task-ordering weight of an NFA byte relative to a DFA byt
 MIN_CHUNK = 256      # shortest speculative chunk (bytes)
 LANE_GROUP = 32      # chunks per LANES task (one per lane)
 # an automaton's chunks run one per lane when its two-byte supersets are this small on
-# average (the lane holds at most native.LANE_CAPACITY states; larger sets spill to warps)
-LANE_PAIR_MEAN = 4.0
+# average: a lane starts from the superset when it has at most native.LANE_CAPACITY
+# states, else from the superset two bytes earlier stepped over the two bytes (up to 64
+# states streamed once); sets that outgrow the lane spill to warps
+LANE_PAIR_MEAN = 32.0
 # resident warps per SM of the lane launch (128-thread CTAs, 8 per SM: csrc/lanes.cu)
 LANE_WARPS_PER_SM = 32
 
