@@ -441,11 +441,36 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
     return load_targets(cur, valid, acc, mk, nm, recs);
 }
 
+// Calls f(edge) for every edge of the lane record r labelled `sym` (or ANY).
+template <typename F>
+__device__ __forceinline__ void for_each_match(const uint4 &r, uint32_t sym,
+                                               const uint16_t *__restrict__ labels,
+                                               const uint2 *__restrict__ ext, F &&f) {
+    if (!(r.x & GBFSM_LANE_SLOW)) {
+        uint32_t m[4];
+        label_matches(r, sym * 0x01010101u, ext, m);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            while (m[w]) {
+                f(r.y + 4u * w + ((uint32_t)(__ffs(m[w]) - 1) >> 3));
+                m[w] &= m[w] - 1u;
+            }
+        }
+    } else {
+        for (uint32_t k = r.y; k < r.z; ++k) {
+            const uint32_t es = __ldg(labels + k);
+            if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) f(k);
+        }
+    }
+}
+
 // Start set of a later chunk at b when the two-byte superset there is too large for a
 // lane: the two-byte superset at b-2 (at most kWideStart members, streamed from
-// pair_lanes) stepped over x[b-2], then x[b-1] -- again a superset of the true set at
-// b, and usually far smaller. Returns false when the wide set is too large or a step
-// matches more than kLaneSlots edges.
+// pair_lanes) stepped over x[b-2] and x[b-1] -- again a superset of the true set at b,
+// and usually far smaller. The intermediate set is never held: each member's targets
+// on x[b-2] are expanded over x[b-1] at once, and only the final edges (distinct, at
+// most kLaneSlots) are kept. Returns false when the wide set or the final set is too
+// large.
 constexpr uint32_t kWideStart = 64;
 
 __device__ inline bool widened_start(const gbfsm_nfa_dev &A, const uint8_t *base, int64_t b,
@@ -458,36 +483,28 @@ __device__ inline bool widened_start(const gbfsm_nfa_dev &A, const uint8_t *base
     const uint32_t pr = __ldg(A.pair_row + key);
     const uint32_t cnt = __ldg(A.pair_row + key + 1) - pr;
     if (cnt > kWideStart) return false;
-    const uint32_t sym = byte_at(base + b - 2);
-    const uint32_t sym4 = sym * 0x01010101u;
+    const uint32_t s1 = byte_at(base + b - 2), s2 = byte_at(base + b - 1);
     uint32_t mk[kLaneSlots];
     int nm = 0;
 #pragma unroll
-    for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0;
+    for (int q = 0; q < kLaneSlots; ++q) mk[q] = 0xFFFFFFFFu;
+    auto add_final = [&](uint32_t k2) {
+        bool seen = false;
+#pragma unroll
+        for (int u = 0; u < kLaneSlots; ++u) seen = seen || mk[u] == k2;
+        if (!seen) add_match(mk, nm, k2);
+    };
     for (uint32_t q = 0; q < cnt && nm <= kLaneSlots; ++q) {
         const uint4 r = ld_lane(A.pair_lanes + pr + q);
-        if (!(r.x & GBFSM_LANE_SLOW)) {
-            uint32_t m[4];
-            label_matches(r, sym4, ext, m);
-#pragma unroll
-            for (int w = 0; w < 4; ++w) {
-                while (m[w]) {
-                    add_match(mk, nm, r.y + 4u * w + ((uint32_t)(__ffs(m[w]) - 1) >> 3));
-                    m[w] &= m[w] - 1u;
-                }
-            }
-        } else {
-            for (uint32_t k = r.y; k < r.z; ++k) {
-                const uint32_t es = __ldg(labels + k);
-                if (es == sym || es == (uint32_t)GBFSM_ANY_SYMBOL) add_match(mk, nm, k);
-            }
-        }
+        for_each_match(r, s1, labels, ext, [&](uint32_t k1) {
+            if (nm > kLaneSlots) return;
+            for_each_match(ld_lane(recs + k1), s2, labels, ext, add_final);
+        });
     }
     if (nm > kLaneSlots) return false;
     bool acc;
     load_targets(cur, valid, acc, mk, nm, recs);
-    if (valid == 0u) return true;
-    return lane_step(cur, valid, acc, byte_at(base + b - 1), labels, recs, ext) >= 0;
+    return true;
 }
 
 // Returns false, writing nothing, when a start superset or a byte's matches exceed
