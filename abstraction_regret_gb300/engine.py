@@ -239,7 +239,8 @@ class PersistentEngine:
             size += 64
         return int(min(size, 1 << 20))
 
-    def make_tasks(self, aut_ids, lengths, starts=None) -> TaskPlan:
+    def make_tasks(self, aut_ids, lengths, starts=None, lane_chunk: int | None = None,
+                   warp_chunk: int | None = None) -> TaskPlan:
         """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
         packed back to back from 0) on automaton ``aut_ids[i]``. Chunk bounds are nominal:
         the kernels move each later chunk's start a few bytes forward to where the
@@ -273,8 +274,9 @@ class PersistentEngine:
             if self.chunk_bytes:
                 chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
             else:
-                chunk_w = self.auto_chunk_bytes(int(lengths[warp_in].sum()))
-                chunk_l = self.auto_lane_chunk_bytes(lengths[lane_in], aut_ids[lane_in])
+                chunk_w = warp_chunk or self.auto_chunk_bytes(int(lengths[warp_in].sum()))
+                chunk_l = lane_chunk or self.auto_lane_chunk_bytes(lengths[lane_in],
+                                                                   aut_ids[lane_in])
             csize[warp_in] = chunk_w
             csize[lane_in] = chunk_l
         # every input of a lane automaton is chunked (a short one is a single exact
@@ -473,6 +475,26 @@ class PersistentEngine:
         return batch_results(flags, lens, kms, tms)
 
 
+class _Part:
+    """One slice of a pipelined batch: inputs [first, last), their task plan (chunk sizes
+    of the whole batch, so that the slices together fill one wave), and a stream and
+    workspace of their own so that slices run concurrently."""
+
+    def __init__(self, engine, aut_ids, lengths, offsets, first, last, padded, whole):
+        self.first, self.last = first, last
+        self.plan = engine.make_tasks(aut_ids[first:last], lengths[first:last],
+                                      starts=offsets[first:last],
+                                      lane_chunk=whole.lane_chunk_bytes or None,
+                                      warp_chunk=whole.chunk_bytes or None)
+        self.tasks = DeviceTasks(engine.device)
+        self.lo = int(offsets[first]) // 16 * 16
+        self.hi = min(padded, -(-int(offsets[last]) // 16) * 16)
+        self.copied = torch.cuda.Event()
+        self.done = torch.cuda.Event()
+        self.stream = torch.cuda.Stream(engine.device)
+        self.workspace = engine.new_workspace()
+
+
 class GraphRunner:
     """A fixed batch captured as one CUDA graph: H2D inputs, the launches, D2H verdicts.
 
@@ -480,37 +502,59 @@ class GraphRunner:
     ``replay`` re-runs it end to end.
     """
 
+    INGEST = ("copy", "zero_copy", "pipelined")
+
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
-                 with_examined: bool = False, zero_copy: bool = False) -> None:
-        """``zero_copy``: the captured graph does not copy the inputs; the kernels read
-        them in place from the pinned host buffer over the host link (NVLink-C2C on
-        GB300). ``kernel_only`` always uses the device copy."""
+                 with_examined: bool = False, ingest: str = "copy", parts: int = 4) -> None:
+        """``ingest`` says how each replay moves the inputs from the pinned host buffer:
+
+        * ``copy``: one copy-engine transfer, then the launches;
+        * ``zero_copy``: no copy, the simulation kernels read the bytes in place over the
+          host link (NVLink-C2C on GB300);
+        * ``pipelined``: the batch is cut into ``parts`` slices of contiguous inputs with
+          about equal bytes, each with its own task plan (the whole batch's chunk sizes)
+          and stream; a slice's launches start as soon as its bytes have arrived, while
+          later slices are still being copied, and the slices run concurrently.
+
+        ``kernel_only`` always runs the whole-batch plan on the device copy."""
+        if ingest not in self.INGEST:
+            raise ValueError(f"ingest must be one of {self.INGEST}")
         self.engine = engine
         dev = engine.device
         n = len(offsets) - 1
         self.n = n
-        lengths = np.diff(np.asarray(offsets, dtype=np.int64))
-        self.task_plan = engine.make_tasks(np.asarray(aut_ids), lengths)
+        offsets = np.asarray(offsets, dtype=np.int64)
+        lengths = np.diff(offsets)
+        aut_ids = np.asarray(aut_ids)
+        self.task_plan = engine.make_tasks(aut_ids, lengths)
         total = int(offsets[-1])
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
         self.h_data.numpy()[:total] = np.asarray(data[:total], dtype=np.uint8)
-        self.h_off = torch.from_numpy(np.asarray(offsets, dtype=np.int64).copy()).pin_memory()
+        self.h_off = torch.from_numpy(offsets.copy()).pin_memory()
         self.h_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, pin_memory=True)
         self.d_data = torch.empty_like(self.h_data, device=dev)
         self.d_data.copy_(self.h_data)
         self.d_off = torch.empty_like(self.h_off, device=dev)
-        self.zero_copy = zero_copy
-        self.host_ptr = native.device_pointer(self.h_data.data_ptr()) if zero_copy else None
+        self.ingest = ingest
+        self.host_ptr = (native.device_pointer(self.h_data.data_ptr())
+                         if ingest == "zero_copy" else None)
         self.d_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, device=dev)
         self.tasks = DeviceTasks(dev)
         self.with_examined = with_examined
         self.stream = torch.cuda.Stream(dev)
-        p = self.task_plan
-        self.h2d_bytes = padded + self.h_off.numel() * 8 + (p.tasks_l.shape[0] +
-                                                             p.tasks_a.shape[0] +
-                                                             p.tasks_b.shape[0]) * 16 + \
-            p.input_ids.size * 4 + p.chunks.shape[0] * 24
+        self.parts: list[_Part] = []
+        if ingest == "pipelined" and n:
+            cut = np.searchsorted(offsets[1:], total * np.arange(1, parts) / parts) + 1
+            bounds = np.unique(np.concatenate([[0], np.minimum(cut, n), [n]]))
+            self.parts = [_Part(engine, aut_ids, lengths, offsets, int(a), int(b), padded,
+                                self.task_plan)
+                          for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+            self.copy_stream = torch.cuda.Stream(dev)
+        plans = [q.plan for q in self.parts] or [self.task_plan]
+        self.h2d_bytes = padded + self.h_off.numel() * 8 + sum(
+            (p.tasks_l.shape[0] + p.tasks_a.shape[0] + p.tasks_b.shape[0]) * 16
+            + p.input_ids.size * 4 + p.chunks.shape[0] * 24 for p in plans)
         self.d2h_bytes = self.h_out.numel() * 4
         self.launches_per_step = 0
         # warm-up outside capture (kernel attributes, occupancy queries, module load)
@@ -522,15 +566,42 @@ class GraphRunner:
             self._body()
         torch.cuda.synchronize(dev)
 
+    def _outputs(self, first: int):
+        ex = self.d_out[2][first:] if self.with_examined else None
+        return self.d_out[0][first:], self.d_out[1][first:], ex
+
     def _body(self) -> None:
         s = torch.cuda.current_stream(self.engine.device)
-        if not self.zero_copy:
-            self.d_data.copy_(self.h_data, non_blocking=True)
         self.d_off.copy_(self.h_off, non_blocking=True)
-        self.tasks.upload(self.task_plan, s)
-        self.launches_per_step = self.engine.launch(
-            self.host_ptr if self.zero_copy else self.d_data, self.d_off, self.tasks,
-            self.d_out[0], self.d_out[1], self.d_out[2] if self.with_examined else None, s)
+        if self.parts:
+            # the small task tables first, so they do not queue behind the input slices
+            for q in self.parts:
+                q.tasks.upload(q.plan, s)
+            start = torch.cuda.Event()
+            start.record(s)
+            self.copy_stream.wait_event(start)
+            with torch.cuda.stream(self.copy_stream):
+                for q in self.parts:
+                    self.d_data[q.lo:q.hi].copy_(self.h_data[q.lo:q.hi], non_blocking=True)
+                    q.copied.record(self.copy_stream)
+            launches = 0
+            for q in self.parts:
+                q.stream.wait_event(q.copied)
+                f, l, ex = self._outputs(q.first)
+                launches += self.engine.launch(self.d_data, self.d_off[q.first:], q.tasks, f, l,
+                                               ex, q.stream, workspace=q.workspace)
+                q.done.record(q.stream)
+            for q in self.parts:
+                s.wait_event(q.done)
+            self.launches_per_step = launches
+        else:
+            if self.ingest == "copy":
+                self.d_data.copy_(self.h_data, non_blocking=True)
+            self.tasks.upload(self.task_plan, s)
+            f, l, ex = self._outputs(0)
+            self.launches_per_step = self.engine.launch(
+                self.host_ptr if self.ingest == "zero_copy" else self.d_data, self.d_off,
+                self.tasks, f, l, ex, s)
         self.h_out.copy_(self.d_out, non_blocking=True)
 
     def replay(self) -> None:
@@ -540,9 +611,11 @@ class GraphRunner:
     def kernel_only(self, stream=None, phases: dict | None = None) -> int:
         """The launches alone on resident inputs (for device-side timing)."""
         stream = stream or torch.cuda.current_stream(self.engine.device)
-        return self.engine.launch(self.d_data, self.d_off, self.tasks, self.d_out[0],
-                                  self.d_out[1], self.d_out[2] if self.with_examined else None,
-                                  stream, phases=phases)
+        if not self.tasks.na + self.tasks.nb + self.tasks.nl and self.task_plan.input_ids.size:
+            self.tasks.upload(self.task_plan, stream)
+        f, l, ex = self._outputs(0)
+        return self.engine.launch(self.d_data, self.d_off, self.tasks, f, l, ex, stream,
+                                  phases=phases)
 
     def verdicts(self):
         h = self.h_out.numpy()

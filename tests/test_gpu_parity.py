@@ -349,3 +349,26 @@ def test_dfa_table_split_over_a_cluster(states):
     a = start_acc.build()
     f, l, _, _, _ = CudaDFAExecutor(a).run_arrays([b"", b"xyz"])
     assert f.tolist() == [1, 1] and l.tolist() == [0, 0]
+
+
+@pytest.mark.parametrize("ingest", ["copy", "zero_copy", "pipelined"])
+def test_graph_runner_ingest_paths(ingest):
+    """A captured step (H2D, launches, D2H) gives the oracle's verdicts on every ingest
+    path, replayed twice; the pipelined path plans each slice on its own."""
+    import torch
+
+    from abstraction_regret_gb300.engine import GraphRunner
+
+    b = W.c3("live", n_inputs=192)
+    eng = PersistentEngine(b.automata)
+    r = GraphRunner(eng, b.aut_ids, b.data, b.offsets, with_examined=True, ingest=ingest,
+                    parts=3)
+    of, ol, oe, _ = O.nfa_batch(b.automata[0], b.data, b.offsets)
+    for _ in range(2):
+        with torch.cuda.stream(r.stream):
+            r.replay()
+        r.stream.synchronize()
+        f, l, e = r.verdicts()
+        assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
+    if ingest == "pipelined":
+        assert len(r.parts) == 3
