@@ -55,6 +55,7 @@ extern "C" gbfsm_status gbfsm_nfa_run_static(const gbfsm_nfa_dev *nfa, const uin
                                              const gbfsm_plan *plan, int32_t *flags,
                                              int32_t *lens, int32_t *examined, void *stream) {
     using namespace gbfsm;
+    if (!nfa) return fail(GBFSM_INVALID_ARG, "gbfsm_nfa_run_static: nfa descriptor is NULL");
     const size_t need = n_inputs > 0 ? gbfsm_nfa_workspace_bytes(nfa, n_inputs, plan) : 0;
     if (need > (size_t)GBFSM_STATIC_SCRATCH_BYTES)
         return fail(GBFSM_INVALID_ARG,

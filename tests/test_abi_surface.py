@@ -104,6 +104,14 @@ def test_invalid_arguments_return_status_codes(lib):
     st = lib.gbfsm_dfa_layout(40000, p, p, 2, p, p, p, None)
     assert st == native.UNSUPPORTED
     assert lib.gbfsm_nfa_workspace_bytes(None, 10, None) == 0
+    io = native.ChunkIO()
+    st = lib.gbfsm_lanes_run(p, 1, p, 4, p, p, ctypes.byref(io), None)
+    assert st == native.INVALID_ARG and "NULL" in native.last_error()
+    assert lib.gbfsm_lanes_run(None, 0, None, 0, None, None, None, None) == native.OK
+    assert lib.gbfsm_lanes_run(p, 1, p, -1, p, p, ctypes.byref(io), None) == native.INVALID_ARG
+    st = lib.gbfsm_nfa_run_static(None, None, None, 4, ctypes.byref(plan), None, None, None,
+                                  None)
+    assert st == native.INVALID_ARG
 
 
 def test_status_mapping_raises_the_reference_exception_types():
