@@ -476,15 +476,17 @@ class PersistentEngine:
 
 
 class _Part:
-    """One slice of a pipelined batch: inputs [first, last), their task plan (chunk sizes
-    of the whole batch, so that the slices together fill one wave), and a stream and
-    workspace of their own so that slices run concurrently."""
+    """One slice of a pipelined batch: inputs [first, last), their task plan (the whole
+    batch's chunk sizes, the lane size scaled by `scale`), and a stream and workspace of
+    their own so that slices run concurrently."""
 
-    def __init__(self, engine, aut_ids, lengths, offsets, first, last, padded, whole):
+    def __init__(self, engine, aut_ids, lengths, offsets, first, last, padded, whole,
+                 scale=1.0):
         self.first, self.last = first, last
+        lane = int(whole.lane_chunk_bytes * scale) // 64 * 64
         self.plan = engine.make_tasks(aut_ids[first:last], lengths[first:last],
                                       starts=offsets[first:last],
-                                      lane_chunk=whole.lane_chunk_bytes or None,
+                                      lane_chunk=max(lane, MIN_CHUNK) if lane else None,
                                       warp_chunk=whole.chunk_bytes or None)
         self.tasks = DeviceTasks(engine.device)
         self.lo = int(offsets[first]) // 16 * 16
@@ -505,16 +507,19 @@ class GraphRunner:
     INGEST = ("copy", "zero_copy", "pipelined")
 
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
-                 with_examined: bool = False, ingest: str = "copy", parts: int = 4) -> None:
+                 with_examined: bool = False, ingest: str = "copy", parts: int = 8,
+                 shrink: float = 0.75) -> None:
         """``ingest`` says how each replay moves the inputs from the pinned host buffer:
 
         * ``copy``: one copy-engine transfer, then the launches;
         * ``zero_copy``: no copy, the simulation kernels read the bytes in place over the
           host link (NVLink-C2C on GB300);
         * ``pipelined``: the batch is cut into ``parts`` slices of contiguous inputs with
-          about equal bytes, each with its own task plan (the whole batch's chunk sizes)
-          and stream; a slice's launches start as soon as its bytes have arrived, while
-          later slices are still being copied, and the slices run concurrently.
+          about equal bytes, each with its own task plan and stream; a slice's launches
+          start as soon as its bytes have arrived, while later slices are still being
+          copied, and the slices run concurrently. Slice k of P uses the whole batch's
+          lane chunk size scaled by 1 - shrink * k / P: a slice that arrives later has
+          less time left, so its lanes get shorter chunks.
 
         ``kernel_only`` always runs the whole-batch plan on the device copy."""
         if ingest not in self.INGEST:
@@ -547,9 +552,10 @@ class GraphRunner:
         if ingest == "pipelined" and n:
             cut = np.searchsorted(offsets[1:], total * np.arange(1, parts) / parts) + 1
             bounds = np.unique(np.concatenate([[0], np.minimum(cut, n), [n]]))
-            self.parts = [_Part(engine, aut_ids, lengths, offsets, int(a), int(b), padded,
-                                self.task_plan)
-                          for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+            spans = [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+            self.parts = [_Part(engine, aut_ids, lengths, offsets, a, b, padded,
+                                self.task_plan, 1.0 - shrink * k / len(spans))
+                          for k, (a, b) in enumerate(spans)]
             self.copy_stream = torch.cuda.Stream(dev)
         plans = [q.plan for q in self.parts] or [self.task_plan]
         self.h2d_bytes = padded + self.h_off.numel() * 8 + sum(
