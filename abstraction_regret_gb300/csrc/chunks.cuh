@@ -326,6 +326,20 @@ __device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4,
     }
 }
 
+// Edge of the lowest remaining marker of m (edge 4w + j of the row starting at rb for
+// bit 7 of byte j of word w), cleared from m. m must have a marker.
+__device__ __forceinline__ uint32_t pop_match(uint32_t (&m)[4], uint32_t rb) {
+    const bool z0 = m[0] != 0u, z1 = m[1] != 0u, z2 = m[2] != 0u;
+    const uint32_t w = z0 ? m[0] : z1 ? m[1] : z2 ? m[2] : m[3];
+    const uint32_t off = z0 ? 0u : z1 ? 4u : z2 ? 8u : 12u;
+    const uint32_t rest = w & (w - 1u);
+    if (z0) m[0] = rest;
+    else if (z1) m[1] = rest;
+    else if (z2) m[2] = rest;
+    else m[3] = rest;
+    return rb + off + ((uint32_t)(__ffs(w) - 1) >> 3);
+}
+
 // The set becomes the distinct targets of the matched edges mk[0 .. nm) (nm <= kLaneSlots),
 // their records loaded together; returns the member count (acc: a member accepts).
 __device__ __forceinline__ int load_targets(uint4 (&cur)[kLaneSlots], uint32_t &valid, bool &acc,
@@ -357,59 +371,44 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
                                          const gbfsm_lane_rec *__restrict__ recs,
                                          const uint2 *__restrict__ ext) {
     const uint32_t sym4 = sym * 0x01010101u;
-    // the common case: one member in the fast form with at most one matching edge
-    if (valid == 1u && !(cur[0].x & GBFSM_LANE_SLOW)) {
-        uint32_t m[4];
-        label_matches(cur[0], sym4, ext, m);
-        const int c = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
+    // The common cases, with little divergence between the lanes of a warp: one or two
+    // members in the fast form (slots 0 and 1) with at most two matching edges between
+    // them. The second member's compare and the second load run only in the lanes
+    // that need them.
+    const bool v1 = (valid >> 1) & 1u;
+    if ((valid & ~3u) == 0u && valid != 0u && !(cur[0].x & GBFSM_LANE_SLOW) &&
+        !(v1 && (cur[1].x & GBFSM_LANE_SLOW))) {
+        uint32_t ma[4], mb[4] = {0u, 0u, 0u, 0u};
+        label_matches(cur[0], sym4, ext, ma);
+        const int ca = __popc(ma[0]) + __popc(ma[1]) + __popc(ma[2]) + __popc(ma[3]);
+        int cb = 0;
+        if (v1) {
+            label_matches(cur[1], sym4, ext, mb);
+            cb = __popc(mb[0]) + __popc(mb[1]) + __popc(mb[2]) + __popc(mb[3]);
+        }
+        const int c = ca + cb;
         if (c == 0) {
             valid = 0;
             acc = false;
             return 0;
         }
-        if (c == 1) {
-            const uint32_t w = m[0] ? m[0] : m[1] ? m[1] : m[2] ? m[2] : m[3];
-            const uint32_t base = m[0] ? 0u : m[1] ? 4u : m[2] ? 8u : 12u;
-            cur[0] = ld_lane(recs + cur[0].y + base + ((uint32_t)(__ffs(w) - 1) >> 3));
-            acc = (cur[0].x & GBFSM_LANE_ACCEPT) != 0u;
-            return 1;
-        }
-    }
-    // the next most common: at most two members, each in the fast form with at most 8
-    // edges, and at most two matching edges between them
-    const bool v0 = valid & 1u, v1 = (valid >> 1) & 1u;
-    const bool small0 = !v0 || (!(cur[0].x & GBFSM_LANE_SLOW) && lane_degree(cur[0].x) <= 8u);
-    const bool small1 = !v1 || (!(cur[1].x & GBFSM_LANE_SLOW) && lane_degree(cur[1].x) <= 8u);
-    if ((valid & ~3u) == 0u && small0 && small1) {
-        const int d0 = v0 ? (int)lane_degree(cur[0].x) : 0;
-        const int d1 = v1 ? (int)lane_degree(cur[1].x) : 0;
-        uint32_t a0 = zero_bytes(cur[0].z ^ sym4) & first_bytes(d0);
-        uint32_t a1 = zero_bytes(cur[0].w ^ sym4) & first_bytes(d0 - 4);
-        uint32_t a2 = zero_bytes(cur[1].z ^ sym4) & first_bytes(d1);
-        uint32_t a3 = zero_bytes(cur[1].w ^ sym4) & first_bytes(d1 - 4);
-        const int c = __popc(a0) + __popc(a1) + __popc(a2) + __popc(a3);
         if (c <= 2) {
             const uint32_t rb0 = cur[0].y, rb1 = cur[1].y;
-            uint32_t e[2];
-#pragma unroll
-            for (int t = 0; t < 2; ++t) {  // the lowest remaining match, then clear it
-                const bool z0 = a0 != 0u, z1 = a1 != 0u, z2 = a2 != 0u;
-                const uint32_t w = z0 ? a0 : z1 ? a1 : z2 ? a2 : a3;
-                e[t] = (z0 ? rb0 : z1 ? rb0 + 4u : z2 ? rb1 : rb1 + 4u) +
-                       ((uint32_t)(__ffs(w) - 1) >> 3);
-                const uint32_t rest = w & (w - 1u);
-                if (z0) a0 = rest;
-                else if (z1) a1 = rest;
-                else if (z2) a2 = rest;
-                else a3 = rest;
+            const uint32_t e0 = ca > 0 ? pop_match(ma, rb0) : pop_match(mb, rb1);
+            if (c == 1) {
+                cur[0] = ld_lane(recs + e0);
+                valid = 1u;
+                acc = (cur[0].x & GBFSM_LANE_ACCEPT) != 0u;
+                return 1;
             }
-            if (c >= 1) cur[0] = ld_lane(recs + e[0]);
-            if (c == 2) cur[1] = ld_lane(recs + e[1]);
-            const bool two = c == 2 && ((cur[0].x ^ cur[1].x) & GBFSM_LANE_STATE_MASK) != 0u;
-            valid = c == 0 ? 0u : two ? 3u : 1u;
-            acc = (c >= 1 && (cur[0].x & GBFSM_LANE_ACCEPT)) ||
-                  (two && (cur[1].x & GBFSM_LANE_ACCEPT));
-            return c == 0 ? 0 : two ? 2 : 1;
+            const uint32_t e1 = ca > 1 ? pop_match(ma, rb0) : pop_match(mb, rb1);
+            const uint4 r0 = ld_lane(recs + e0), r1 = ld_lane(recs + e1);
+            const bool two = ((r0.x ^ r1.x) & GBFSM_LANE_STATE_MASK) != 0u;
+            cur[0] = r0;
+            cur[1] = r1;
+            valid = two ? 3u : 1u;
+            acc = (r0.x & GBFSM_LANE_ACCEPT) || (two && (r1.x & GBFSM_LANE_ACCEPT));
+            return two ? 2 : 1;
         }
     }
     uint32_t mk[kLaneSlots];
