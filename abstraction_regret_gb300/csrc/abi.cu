@@ -223,6 +223,8 @@ gbfsm_status gbfsm_host_device_pointer(void *host, void **device) {
     return GBFSM_OK;
 }
 
+int32_t gbfsm_lanes_warps_per_sm(void) { return lanes_warps_per_sm(); }
+
 gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
                              const gbfsm_task *tasks, int32_t n_tasks, const uint8_t *data,
                              const int64_t *offsets, const gbfsm_chunk_io *chunk_io,

@@ -71,6 +71,7 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
                                const gbfsm_chunk_io *chunk_io, int32_t *flags,
                                int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream);
+int lanes_warps_per_sm();
 gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream);

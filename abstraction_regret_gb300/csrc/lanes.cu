@@ -46,6 +46,15 @@ __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
 
 }  // namespace
 
+int lanes_warps_per_sm() {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, lanes_kernel, kLanesThreads, 0) !=
+        cudaSuccess)
+        blocks = 0;
+    cudaGetLastError();
+    return blocks * (kLanesThreads / 32);
+}
+
 gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream) {

@@ -51,7 +51,8 @@ LANE_GROUP = 32      # chunks per LANES task (one per lane)
 # states, else from the superset two bytes earlier stepped over the two bytes (up to 64
 # states streamed once); sets that outgrow the lane spill to warps
 LANE_PAIR_MEAN = 32.0
-# resident warps per SM of the lane launch (128-thread CTAs, 8 per SM: csrc/lanes.cu)
+# resident warps per SM of the lane launch when the device is not asked (128-thread
+# CTAs, 8 per SM: csrc/lanes.cu)
 LANE_WARPS_PER_SM = 32
 
 
@@ -201,6 +202,8 @@ class PersistentEngine:
             self.table = torch.from_numpy(raw).to(self.device)
             props = torch.cuda.get_device_properties(self.device)
         self.sm_count = props.multi_processor_count
+        with torch.cuda.device(self.device):
+            self.lane_warps_per_sm = int(lib.gbfsm_lanes_warps_per_sm()) or LANE_WARPS_PER_SM
         self.resident_warps = self.sm_count * self.ctas_per_sm * (block_threads // 32)
         self._staging = Staging(self.device)
         self._results = Results(self.device)
@@ -221,7 +224,7 @@ class PersistentEngine:
         warps, so the batch runs in one full wave. A lane's steps are dependent L2 round
         trips: once every lane is busy, finer chunks only add per-chunk work, and a second
         partial wave adds its whole duration."""
-        warps = self.sm_count * LANE_WARPS_PER_SM
+        warps = self.sm_count * getattr(self, "lane_warps_per_sm", LANE_WARPS_PER_SM)
         lengths = np.asarray(lengths, dtype=np.int64)
         aut = np.asarray(aut, dtype=np.int64)
         if lengths.size == 0:

@@ -170,6 +170,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_run_dfa_bytes": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                            _vp]),
     "gbfsm_host_device_pointer": (ctypes.c_int, [_vp, _P(_vp)]),
+    "gbfsm_lanes_warps_per_sm": (_i32, []),
     "gbfsm_lanes_run": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _P(ChunkIO), _vp]),
     "gbfsm_nfa_run_static": (ctypes.c_int, [_P(NfaDev), _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                             _vp, _vp]),

@@ -328,6 +328,11 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
  * counterpart in the reference (which copies every input, common.cuh:150-159). */
 gbfsm_status gbfsm_host_device_pointer(void *host, void **device);
 
+/* Resident warps per SM of the lane launch on the current device (0 when it cannot run):
+ * a batch whose LANES tasks fit sm_count times this runs in one wave. No counterpart in
+ * the reference. */
+int32_t gbfsm_lanes_warps_per_sm(void);
+
 /* Run LANES tasks (one warp per task, one chunk per lane), writing chunk records and
  * appending chunks that outgrow a lane to chunk_io->overflow_tasks (the caller zeroes
  * overflow_count first). data/offsets as for gbfsm_persistent_run (contiguous inputs:
