@@ -306,24 +306,31 @@ __device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
 
 // Byte markers of the first k (< 0: none, >= 4: all four) bytes of a word.
 __device__ __forceinline__ uint32_t first_bytes(int k) {
-    return k >= 4 ? 0x80808080u : k <= 0 ? 0u : 0x80808080u & ((1u << (8 * k)) - 1u);
+    // shr.b32 clamps shift counts above 32 to 32, which yields 0 (k <= 0)
+    const uint32_t shift = 32u - 8u * (uint32_t)min(max(k, 0), 4);
+    uint32_t r;
+    asm("shr.b32 %0, %1, %2;" : "=r"(r) : "r"(0x80808080u), "r"(shift));
+    return r;
 }
 
 // Markers (bit 7 of byte j of word w: edge 4w + j) of the labels of a fast-form record
 // equal to the byte: edges 0..7 from the record, edges 8..15 from the ext table.
-__device__ __forceinline__ void label_matches(const uint4 &r, uint32_t sym4,
-                                              const uint2 *__restrict__ ext,
-                                              uint32_t (&m)[4]) {
+// Returns the number of markers.
+__device__ __forceinline__ int label_matches(const uint4 &r, uint32_t sym4,
+                                             const uint2 *__restrict__ ext, uint32_t (&m)[4]) {
     const int deg = (int)lane_degree(r.x);
     m[0] = zero_bytes(r.z ^ sym4) & first_bytes(deg);
     m[1] = zero_bytes(r.w ^ sym4) & first_bytes(deg - 4);
     m[2] = 0u;
     m[3] = 0u;
+    int c = __popc(m[0]) + __popc(m[1]);
     if (deg > 8) {
         const uint2 h = __ldg(ext + (r.x & GBFSM_LANE_STATE_MASK));
         m[2] = zero_bytes(h.x ^ sym4) & first_bytes(deg - 8);
         m[3] = zero_bytes(h.y ^ sym4) & first_bytes(deg - 12);
+        c += __popc(m[2]) + __popc(m[3]);
     }
+    return c;
 }
 
 // Edge of the lowest remaining marker of m (edge 4w + j of the row starting at rb for
@@ -379,13 +386,8 @@ __device__ __forceinline__ int lane_step(uint4 (&cur)[kLaneSlots], uint32_t &val
     if ((valid & ~3u) == 0u && valid != 0u && !(cur[0].x & GBFSM_LANE_SLOW) &&
         !(v1 && (cur[1].x & GBFSM_LANE_SLOW))) {
         uint32_t ma[4], mb[4] = {0u, 0u, 0u, 0u};
-        label_matches(cur[0], sym4, ext, ma);
-        const int ca = __popc(ma[0]) + __popc(ma[1]) + __popc(ma[2]) + __popc(ma[3]);
-        int cb = 0;
-        if (v1) {
-            label_matches(cur[1], sym4, ext, mb);
-            cb = __popc(mb[0]) + __popc(mb[1]) + __popc(mb[2]) + __popc(mb[3]);
-        }
+        const int ca = label_matches(cur[0], sym4, ext, ma);
+        const int cb = v1 ? label_matches(cur[1], sym4, ext, mb) : 0;
         const int c = ca + cb;
         if (c == 0) {
             valid = 0;
