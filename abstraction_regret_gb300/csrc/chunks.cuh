@@ -246,6 +246,44 @@ __device__ inline void run_chunk(const gbfsm_nfa_dev &nfa, const Rows &R, WarpSc
 }
 
 // ---- lane chunk (one chunk per thread; up to kLaneSlots states) ----------------------------
+
+// Sequential 4-byte words of a byte range starting at any alignment: aligned 16-byte
+// blocks read one block ahead (never past `end`), each word put together by one funnel
+// shift of two aligned words.
+struct WordStream {
+    const uint8_t *blk;
+    const uint8_t *end;
+    uint4 cur, nxt;
+    uint32_t wi;  // aligned word (0..3) of cur holding the next byte
+    uint32_t sh;  // 8 x the byte offset of the next byte in that word
+
+    __device__ __forceinline__ static uint32_t word(const uint4 &v, uint32_t i) {
+        return i == 0u ? v.x : i == 1u ? v.y : i == 2u ? v.z : v.w;
+    }
+
+    __device__ __forceinline__ void init(const uint8_t *p, const uint8_t *e) {
+        end = e;
+        const uint64_t a = reinterpret_cast<uint64_t>(p);
+        blk = reinterpret_cast<const uint8_t *>(a & ~15ull);
+        wi = (uint32_t)((a >> 2) & 3u);
+        sh = (uint32_t)(a & 3u) * 8u;
+        cur = ld_stream16(blk);
+        nxt = (blk + 16 < end) ? ld_stream16(blk + 16) : make_uint4(0, 0, 0, 0);
+    }
+
+    __device__ __forceinline__ uint32_t next_word() {
+        const uint32_t lo = word(cur, wi);
+        const uint32_t hi = wi == 3u ? nxt.x : word(cur, wi + 1u);
+        const uint32_t w = __funnelshift_r(lo, hi, sh);
+        if (++wi == 4u) {
+            wi = 0u;
+            blk += 16;
+            cur = nxt;
+            nxt = (blk + 16 < end) ? ld_stream16(blk + 16) : make_uint4(0, 0, 0, 0);
+        }
+        return w;
+    }
+};
 //
 // The set is kept as the lane records (gbfsm_lane_rec) of its members, slot q valid when
 // bit q of `valid` is set. Per byte: find each member's edges labelled with the byte --
@@ -586,13 +624,14 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         for (int q = 0; q < kCheckpoints; ++q)
             if (q == c) counts[q] = m;
     }
-    // the rest: no checkpoints, and any accept ends the run
-    while (!stopped && j < len) {
-        const uint32_t sym = bytes.next();
+    // The rest: no checkpoints, and any accept ends the run. Four bytes per word; the
+    // last (at most three) bytes one at a time. step() returns 1 to stop, -1 when the
+    // set outgrew the lane.
+    auto step = [&](uint32_t sym) -> int {
         ++j;
         bool acc;
         m = lane_step(cur, valid, acc, sym, labels, recs, ext);
-        if (m < 0) return false;
+        if (m < 0) return -1;
         if (m == 0) {
             dead_at = b32 + j;
             stopped = true;
@@ -601,7 +640,23 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
             else note_accept(acc_after, j, b32 + j);
             stopped = true;
         }
+        return stopped ? 1 : 0;
+    };
+    if (!stopped && len - j >= 4) {
+        WordStream words;
+        words.init(base + b + j, base + e);
+        while (!stopped && len - j >= 4) {
+            const uint32_t w4 = words.next_word();
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int r = step((w4 >> (8 * t)) & 0xFFu);
+                if (r < 0) return false;
+                if (r) break;
+            }
+        }
     }
+    while (!stopped && j < len)
+        if (step(byte_at(base + b + j)) < 0) return false;
 #pragma unroll
     for (int c = 0; c < kCheckpoints; ++c) {
         rec->counts[c] = counts[c];
