@@ -374,14 +374,22 @@ __device__ __forceinline__ int label_matches(const uint4 &r, uint32_t sym4,
 // Edge of the lowest remaining marker of m (edge 4w + j of the row starting at rb for
 // bit 7 of byte j of word w), cleared from m. m must have a marker.
 __device__ __forceinline__ uint32_t pop_match(uint32_t (&m)[4], uint32_t rb) {
-    const bool z0 = m[0] != 0u, z1 = m[1] != 0u, z2 = m[2] != 0u;
-    const uint32_t w = z0 ? m[0] : z1 ? m[1] : z2 ? m[2] : m[3];
-    const uint32_t off = z0 ? 0u : z1 ? 4u : z2 ? 8u : 12u;
-    const uint32_t rest = w & (w - 1u);
-    if (z0) m[0] = rest;
-    else if (z1) m[1] = rest;
-    else if (z2) m[2] = rest;
-    else m[3] = rest;
+    uint32_t w, off;
+    if (m[0] | m[1]) {  // edges 0..7: almost every match
+        const bool z0 = m[0] != 0u;
+        w = z0 ? m[0] : m[1];
+        off = z0 ? 0u : 4u;
+        const uint32_t rest = w & (w - 1u);
+        if (z0) m[0] = rest;
+        else m[1] = rest;
+    } else {
+        const bool z2 = m[2] != 0u;
+        w = z2 ? m[2] : m[3];
+        off = z2 ? 8u : 12u;
+        const uint32_t rest = w & (w - 1u);
+        if (z2) m[2] = rest;
+        else m[3] = rest;
+    }
     return rb + off + ((uint32_t)(__ffs(w) - 1) >> 3);
 }
 
