@@ -64,6 +64,8 @@ def parse_args(argv=None):
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline measurement (used for profiling)")
+    ap.add_argument("--extras", default="plain,dfa,c4,serving",
+                    help="comma-separated extra sections after the headline")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the c5 serving trace (0: skip the serving section)")
     ap.add_argument("--slo-ms", type=float, default=50.0,
@@ -328,7 +330,8 @@ def main(argv=None) -> int:
     e2e_other = {k: v for k, v in paths.items() if k != best}
 
     extras = {}
-    if not args.skip_extras and rank == 0:
+    sections = set() if args.skip_extras else set(filter(None, args.extras.split(",")))
+    if "plain" in sections and rank == 0:
         # plain single launch over the whole batch (the autotuned plain plan)
         plain = CudaNFAExecutor(nfa, "compact", dev)
         d_out = torch.zeros((3, batch.n_inputs), dtype=torch.int32, device=dev)
@@ -361,8 +364,9 @@ def main(argv=None) -> int:
         extras["speedup_vs_plain_per_input"] = value / world / per_input_gbps
         extras["speedup_vs_plain_single_launch"] = value / world / extras["plain_single_launch"]["value"]
         del plain, d_out
-        for k in [k for k in runners if k != "copy"]:
-            del runners[k]
+    for k in [k for k in runners if k != "copy"]:
+        del runners[k]
+    if "dfa" in sections and rank == 0:
         # DFA walk on c2 (literal and sustained)
         for variant in ("literal", "sustained"):
             b2 = W.c2(variant)
@@ -379,9 +383,10 @@ def main(argv=None) -> int:
                 "examined_GBps": int(oe.sum()) / (d_ms * 1e-3) / 1e9,
                 "ms": d_ms, "examined_bytes": int(oe.sum()), "checked": int(of.size)}
             del r2, ex2, b2
+    if "c4" in sections and rank == 0:
         extras["c4_multi_automaton"] = c4_section(dev, max(2, args.steps // 2))
-        if args.serve_requests > 0:
-            extras["serving"] = serving_section(dev, args.serve_requests, args.slo_ms)
+    if "serving" in sections and rank == 0 and args.serve_requests > 0:
+        extras["serving"] = serving_section(dev, args.serve_requests, args.slo_ms)
 
     cpu = cpu_reference(batch) if rank == 0 else None
 
