@@ -807,7 +807,7 @@ __device__ inline Verdict serial_fixup(WarpNfa<false> &w, const uint8_t *base, i
             if (rk.dead_at >= 0) return decided(0, rk.dead_at);
             if (rk.end_count >= 0) {
                 w.cleanup();
-                w.init_recs(recs[first + k].end_recs, rk.end_count);
+                w.init_recs(recs[first + k].end_recs, min(rk.end_count, kEndCap));
             } else {
                 while (b + j < e) w.step(byte_at(base + b + j++));  // no event can occur here
             }
@@ -855,7 +855,8 @@ __device__ inline Verdict run_fixup(const gbfsm_nfa_dev &nfa, const Rows &R, War
     WarpNfa<false> w(nfa, R, S);
     int start;
     if (last_rec >= 0) {
-        w.init_recs(recs[first + last_rec].end_recs, recs[first + last_rec].end_count);
+        w.init_recs(recs[first + last_rec].end_recs,
+                    min(recs[first + last_rec].end_count, kEndCap));
         start = last_rec + 1;
     } else {  // the first chunk's final set was not recorded: recompute it exactly
         w.init_start();

@@ -32,9 +32,16 @@ __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
     const int cid = task.first + lane;
     const gbfsm_chunk ch = io.chunks[cid];
     const int64_t off = offsets[ch.input];
-    const gbfsm_nfa_dev &A = table[task.automaton].nfa;
-    const Bounds bd = chunk_bounds(io, A, data + off, cid, off);
-    if (!lane_chunk(A, data + off, bd.b, bd.e, bd.ov_end, ch.index, io.records + cid)) {
+    const gbfsm_automaton &T = table[task.automaton];
+    const gbfsm_nfa_dev &A = T.nfa;
+    if (T.kind != 0) return;  // LANES tasks of a DFA are ignored
+    const bool lane_tables = A.lane_edges != nullptr && A.pair_row != nullptr;
+    bool done = false;
+    if (lane_tables) {
+        const Bounds bd = chunk_bounds(io, A, data + off, cid, off);
+        done = lane_chunk(A, data + off, bd.b, bd.e, bd.ov_end, ch.index, io.records + cid);
+    }
+    if (!done) {
         gbfsm_task spill;
         spill.automaton = task.automaton;
         spill.first = cid;

@@ -97,8 +97,11 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
             R.eps_row = nfa.eps_row;
             R.eps_edges = nfa.eps_edges;
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
+            if (task.kind == GBFSM_TASK_LANES) continue;  // gbfsm_lanes_run's tasks
             if (task.kind == GBFSM_TASK_CHUNK) {
                 const gbfsm_chunk ch = chunks[task.first];
+                // a later chunk needs the one-byte supersets; without them it is not run
+                if (ch.index > 0 && nfa.first_row == nullptr) continue;
                 const int64_t off = offsets[ch.input];
                 if (S.C == 0) S.C = min(L.C, 32);  // speculation keeps small sets listed
                 const Bounds bd = chunk_bounds(io, nfa, data + off, task.first, off);

@@ -305,10 +305,12 @@ typedef struct gbfsm_chunk_io {
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan);
 
-/* Run `n_tasks` tasks. table/tasks/input_ids (and the chunk_io buffers, needed only by
- * CHUNK, LANES and FIXUP tasks) are device arrays. Speculative chunking takes up to three
- * calls on one stream: the LANES / CHUNK tasks (with any WHOLE tasks); the overflow queue
- * (tasks = overflow_tasks, task_count = overflow_count); then the FIXUP tasks. Input i is
+/* Run `n_tasks` WHOLE, CHUNK and FIXUP tasks (LANES tasks are skipped: they belong to
+ * gbfsm_lanes_run). table/tasks/input_ids (and the chunk_io buffers, needed only by
+ * CHUNK and FIXUP tasks) are device arrays. Speculative chunking takes up to four calls on
+ * one stream: gbfsm_lanes_run for the LANES tasks; this call for the CHUNK tasks (with
+ * any WHOLE tasks); this call for the overflow queue (tasks = overflow_tasks,
+ * task_count = overflow_count); then this call for the FIXUP tasks. Input i is
  * data[offsets[i] .. ends[i]) when `ends` is non-NULL (spans anywhere in `data`, e.g.
  * requests left in place in a pinned host pool that the device reads directly), else
  * data[offsets[i] .. offsets[i+1]). Results are written by input index. workspace
@@ -335,7 +337,9 @@ int32_t gbfsm_lanes_warps_per_sm(void);
 
 /* Run LANES tasks (one warp per task, one chunk per lane), writing chunk records and
  * appending chunks that outgrow a lane to chunk_io->overflow_tasks (the caller zeroes
- * overflow_count first). data/offsets as for gbfsm_persistent_run (contiguous inputs:
+ * overflow_count first). A task whose automaton is an NFA without lane tables
+ * (gbfsm_nfa_dev.lane_edges and pair_row) sends all its chunks to the overflow queue; a
+ * task of a DFA is ignored. data/offsets as for gbfsm_persistent_run (contiguous inputs:
  * input i starts at offsets[i]). No counterpart in the reference. */
 gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
                              const gbfsm_task *tasks, int32_t n_tasks, const uint8_t *data,
