@@ -478,6 +478,17 @@ class PersistentEngine:
         return batch_results(flags, lens, kms, tms)
 
 
+def slice_bounds(offsets: np.ndarray, parts: int) -> list[tuple[int, int]]:
+    """Contiguous input ranges [a, b) covering every input, cut where the cumulative bytes
+    cross multiples of total / parts (empty ranges dropped)."""
+    offsets = np.asarray(offsets, dtype=np.int64)
+    n = offsets.size - 1
+    total = int(offsets[-1])
+    cut = np.searchsorted(offsets[1:], total * np.arange(1, parts) / parts) + 1
+    bounds = np.unique(np.concatenate([[0], np.minimum(cut, n), [n]]))
+    return [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+
+
 class _Part:
     """One slice of a pipelined batch: inputs [first, last), their task plan (the whole
     batch's chunk sizes, the lane size scaled by `scale`), and a stream and workspace of
@@ -553,9 +564,7 @@ class GraphRunner:
         self.stream = torch.cuda.Stream(dev)
         self.parts: list[_Part] = []
         if ingest == "pipelined" and n:
-            cut = np.searchsorted(offsets[1:], total * np.arange(1, parts) / parts) + 1
-            bounds = np.unique(np.concatenate([[0], np.minimum(cut, n), [n]]))
-            spans = [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+            spans = slice_bounds(offsets, parts)
             self.parts = [_Part(engine, aut_ids, lengths, offsets, a, b, padded,
                                 self.task_plan, 1.0 - shrink * k / len(spans))
                           for k, (a, b) in enumerate(spans)]

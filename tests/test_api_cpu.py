@@ -245,3 +245,88 @@ def test_lane_records_pack_edges_8_to_15_separately():
     words = [int(recs[0, 2]), int(recs[0, 3]), int(ext[0, 0]), int(ext[0, 1])]
     packed = [(words[k // 4] >> (8 * (k % 4))) & 0xFF for k in range(12)]
     assert packed == [int(s) for s in got]
+
+
+def _planner(kinds, lane_ok, can_chunk, chunk_bytes=0):
+    """A PersistentEngine with only the attributes its task planner reads (no device)."""
+    from abstraction_regret_gb300.engine import PersistentEngine
+    from abstraction_regret_gb300.registry import Kind
+
+    eng = PersistentEngine.__new__(PersistentEngine)
+    eng.automata = [object()] * len(kinds)
+    eng.kinds = [Kind.NFA if k == "nfa" else Kind.DFA for k in kinds]
+    eng.lane_ok = np.asarray(lane_ok, dtype=bool)
+    eng.can_chunk = np.asarray(can_chunk, dtype=bool)
+    eng.chunk_bytes = chunk_bytes
+    eng.sm_count, eng.lane_warps_per_sm, eng.resident_warps = 152, 32, 152 * 16
+    return eng
+
+
+def test_task_plan_covers_every_input_exactly_once():
+    """Lane chunks tile their inputs in even chunks, LANES tasks hold <= 32 chunks of one
+    automaton, warp chunks and fix-ups match, and every input is resolved exactly once."""
+    from abstraction_regret_gb300 import native
+
+    rng = np.random.default_rng(4)
+    # automaton 0: lanes; 1: warp chunks only; 2: not chunkable; 3: DFA
+    eng = _planner(["nfa", "nfa", "nfa", "dfa"], [1, 0, 0, 0], [1, 1, 0, 0], chunk_bytes=512)
+    n = 300
+    aut = rng.integers(0, 4, n)
+    lengths = rng.integers(0, 6000, n)
+    starts = np.zeros(n, np.int64)
+    np.cumsum(lengths[:-1], out=starts[1:])
+    p = eng.make_tasks(aut, lengths)
+    ch = p.chunks
+    resolved = np.zeros(n, np.int64)
+    # fix-ups: one per chunked input, its chunks tile the input
+    for a_, first, count, kind in p.tasks_b.tolist():
+        assert kind == native.TASK_FIXUP
+        c = ch[first:first + count]
+        i = int(c["input"][0])
+        assert (c["input"] == i).all() and list(c["index"]) == list(range(count))
+        assert c["begin"][0] == starts[i] and c["end"][-1] == starts[i] + lengths[i]
+        assert (c["begin"][1:] == c["end"][:-1]).all()
+        if count > 1:
+            size = c["end"] - c["begin"]
+            assert size.max() <= 512 and size.min() > 256
+        assert aut[i] == a_
+        resolved[i] += 1
+    # lane chunks first, grouped in LANES tasks of one automaton
+    covered = np.zeros(ch.shape[0], np.int64)
+    for a_, first, count, kind in p.tasks_l.tolist():
+        assert kind == native.TASK_LANES and 1 <= count <= 32 and first + count <= p.lane_chunks
+        assert (aut[ch["input"][first:first + count]] == a_).all() and a_ == 0
+        covered[first:first + count] += 1
+    whole_nfa = 0
+    for a_, first, count, kind in p.tasks_a.tolist():
+        if kind == native.TASK_CHUNK:
+            assert count == 1 and first >= p.lane_chunks and a_ == 1
+            covered[first] += 1
+        else:
+            assert kind == native.TASK_WHOLE
+            ids = p.input_ids[first:first + count]
+            assert (aut[ids] == a_).all()
+            if a_ == 3:
+                assert count <= 32
+            else:
+                assert count == 1
+                whole_nfa += 1
+            resolved[ids] += 1
+    assert (covered == 1).all()
+    assert (resolved == 1).all()
+    assert sorted(p.input_ids.tolist()) == list(range(n))
+
+
+def test_pipeline_slices_are_contiguous_and_balanced():
+    from abstraction_regret_gb300.engine import slice_bounds
+
+    lengths = np.random.default_rng(1).integers(1, 10000, 500)
+    off = np.zeros(501, np.int64)
+    np.cumsum(lengths, out=off[1:])
+    spans = slice_bounds(off, 8)
+    assert spans[0][0] == 0 and spans[-1][1] == 500
+    assert all(a < b for a, b in spans) and all(spans[k][1] == spans[k + 1][0]
+                                                for k in range(len(spans) - 1))
+    sizes = [off[b] - off[a] for a, b in spans]
+    assert len(spans) == 8 and max(sizes) < 1.3 * off[-1] / 8
+    assert slice_bounds(off[:2], 8) == [(0, 1)]
