@@ -249,9 +249,9 @@ gbfsm_status launch_dfa_walk(const gbfsm_dfa_dev &d, const gbfsm_plan &p, const 
         const int fit = cluster_capacity(ctas, 32);
         if (fit > 0) {
             // spread the inputs over every co-resident cluster before stacking them
+            // (a partial warp is fine: every co-resident cluster gets chains)
             const int per_cta = (n_inputs + fit * ctas - 1) / (fit * ctas);
-            int t = ((per_cta + 31) / 32) * 32;
-            t = t < 32 ? 32 : t > 256 ? 256 : t;
+            const int t = per_cta < 32 ? 32 : per_cta > 256 ? 256 : per_cta;
             if (t == 32 || cluster_capacity(ctas, t) > 0)
                 return launch_cluster(d, ctas, t, data, offsets, n_inputs, flags, lens,
                                       examined, stream);
