@@ -64,7 +64,7 @@ def parse_args(argv=None):
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline measurement (used for profiling)")
-    ap.add_argument("--extras", default="plain,dfa,c4,serving",
+    ap.add_argument("--extras", default="plain,c1,dfa,c4,serving",
                     help="comma-separated extra sections after the headline")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the c5 serving trace (0: skip the serving section)")
@@ -383,6 +383,8 @@ def main(argv=None) -> int:
                 "examined_GBps": int(oe.sum()) / (d_ms * 1e-3) / 1e9,
                 "ms": d_ms, "examined_bytes": int(oe.sum()), "checked": int(of.size)}
             del r2, ex2, b2
+    if "c1" in sections and rank == 0:
+        extras["c1_plain_nfa"] = c1_section(dev, max(2, args.steps // 2))
     if "c4" in sections and rank == 0:
         extras["c4_multi_automaton"] = c4_section(dev, max(2, args.steps // 2))
     if "serving" in sections and rank == 0 and args.serve_requests > 0:
@@ -448,6 +450,48 @@ def main(argv=None) -> int:
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def c1_section(dev, steps: int) -> dict:
+    """c1: the 1024-state NFA on 64 inputs of 4 KiB (live and sustained random walks;
+    the literal inputs die after about one byte), one engine step and one plain launch,
+    both checked against the oracle first."""
+    import torch
+
+    from abstraction_regret_gb300 import workloads as W
+    from abstraction_regret_gb300.engine import GraphRunner, PersistentEngine
+    from abstraction_regret_gb300.executors import CudaNFAExecutor
+    from oracle import oracle as O
+
+    out = {}
+    for variant in ("live", "sustained"):
+        b = W.c1(variant)
+        nfa = b.automata[0]
+        of, ol, oe, _ = O.nfa_batch(nfa, b.data, b.offsets)
+        r = GraphRunner(PersistentEngine([nfa], dev), b.aut_ids, b.data, b.offsets,
+                        with_examined=True)
+        with torch.cuda.stream(r.stream):
+            r.replay()
+        r.stream.synchronize()
+        f, l, ex = r.verdicts()
+        if not (np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(ex, oe)):
+            raise SystemExit(f"c1-{variant}: engine differs from the oracle")
+        with torch.cuda.stream(r.stream):
+            ms = time_launches(lambda: r.kernel_only(r.stream), r.stream, steps, 3)
+        plain = CudaNFAExecutor(nfa, "auto", dev)
+        d_out = torch.zeros((3, b.n_inputs), dtype=torch.int32, device=dev)
+        with torch.cuda.stream(r.stream):
+            plain_ms = time_launches(lambda: plain.launch(r.d_data, r.d_off, b.n_inputs,
+                                                          d_out[0], d_out[1], None, r.stream),
+                                     r.stream, steps, 3)
+        if not np.array_equal(d_out[0].cpu().numpy(), of):
+            raise SystemExit(f"c1-{variant}: plain launch differs from the oracle")
+        out[variant] = {"engine_GBps": b.total_bytes / (ms * 1e-3) / 1e9, "engine_ms": ms,
+                        "plain_GBps": b.total_bytes / (plain_ms * 1e-3) / 1e9,
+                        "plain_ms": plain_ms, "offered_bytes": int(b.total_bytes),
+                        "checked": int(f.size)}
+        del r, plain
+    return out
 
 
 def c4_section(dev, steps: int) -> dict:
