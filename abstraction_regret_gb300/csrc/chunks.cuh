@@ -632,9 +632,20 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
         for (int q = 0; q < kCheckpoints; ++q)
             if (q == c) counts[q] = m;
     }
-    // The rest: no checkpoints, and any accept ends the run. Four bytes per word; the
-    // last (at most three) bytes one at a time. step() returns 1 to stop, -1 when the
-    // set outgrew the lane.
+    // The checkpoint sizes are final now, and so are the first accepts found so far:
+    // write them, keeping only which accepts are still open, so that the long loop below
+    // holds no arrays.
+    uint32_t open_acc = 0;  // (a first chunk records only its own first accept)
+#pragma unroll
+    for (int c = 0; c < kCheckpoints; ++c) {
+        rec->counts[c] = counts[c];
+        rec->acc_after[c] = acc_after[c];
+        if (acc_after[c] < 0 && (index > 0 || c == 0)) open_acc |= 1u << c;
+    }
+    // The rest: no checkpoints, and any accept ends the run (it is the first accept
+    // after every checkpoint still open, all of which lie before it). Four bytes per
+    // word; the last (at most three) bytes one at a time. step() returns 1 to stop, -1
+    // when the set outgrew the lane.
     auto step = [&](uint32_t sym) -> int {
         ++j;
         bool acc;
@@ -644,8 +655,8 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
             dead_at = b32 + j;
             stopped = true;
         } else if (acc) {
-            if (index == 0) acc_after[0] = b32 + j;
-            else note_accept(acc_after, j, b32 + j);
+            for (int c = 0; c < kCheckpoints; ++c)
+                if ((open_acc >> c) & 1u) rec->acc_after[c] = b32 + j;
             stopped = true;
         }
         return stopped ? 1 : 0;
@@ -665,11 +676,6 @@ __device__ inline bool lane_chunk(const gbfsm_nfa_dev &A, const uint8_t *base, i
     }
     while (!stopped && j < len)
         if (step(byte_at(base + b + j)) < 0) return false;
-#pragma unroll
-    for (int c = 0; c < kCheckpoints; ++c) {
-        rec->counts[c] = counts[c];
-        rec->acc_after[c] = acc_after[c];
-    }
     rec->dead_at = dead_at;
     rec->end_count = stopped ? -1 : m;
     rec->begin = b;
