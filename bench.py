@@ -149,6 +149,25 @@ class ClockSampler:
 # ---- measurements ---------------------------------------------------------------------------
 
 
+def max_over_ranks(x: float, device, world: int) -> float:
+    """The slowest rank's time: every replica's step must be over for the job's step."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(offered_bytes: int, ms: float, world: int) -> float:
+    """Whole-job GB/s of `world` replicas, each processing `offered_bytes` per step, at
+    the slowest rank's step time (replicas only: inputs are independent, nothing is
+    exchanged)."""
+    return offered_bytes * world / (ms * 1e-3) / 1e9
+
+
 def time_launches(fn, stream, steps: int, warmup: int):
     """Mean ms per call of ``fn`` over ``steps`` calls (CUDA events on ``stream``)."""
     import torch
@@ -296,11 +315,8 @@ def main(argv=None) -> int:
         ms = e0.elapsed_time(e1) / args.steps
         torch.cuda.synchronize()
     barrier()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = offered * world / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(ms, dev, world)
+    value = replica_throughput(offered, ms, world)
     phase_ms = {k: float(np.mean([ev[2 * i].elapsed_time(ev[2 * i + 1])
                                   for i in range(len(ev) // 2)]))
                 for k, ev in phases.items()}
@@ -317,11 +333,8 @@ def main(argv=None) -> int:
     for name, r in runners.items():
         with torch.cuda.stream(r.stream):
             e2e_ms = time_launches(r.replay, r.stream, args.steps, args.warmup)
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        paths[name] = {"value": offered * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+        e2e_ms = max_over_ranks(e2e_ms, dev, world)
+        paths[name] = {"value": replica_throughput(offered, e2e_ms, world), "unit": "GB/s",
                        "h2d_bytes_per_step": int(r.h2d_bytes),
                        "d2h_bytes_per_step": int(r.d2h_bytes), "ms_per_step": e2e_ms,
                        "path": describe[name]}
