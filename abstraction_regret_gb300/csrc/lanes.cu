@@ -2,7 +2,8 @@
 //
 // Each warp takes one LANES task (up to 32 chunks of one automaton) and each lane runs one
 // chunk with lane_chunk() (chunks.cuh): a set of at most kLaneSlots states held as their
-// records in registers, one L1 label scan and one batched L2 record load per byte. A chunk
+// lane records in registers, matched against each byte by byte-wise compares of their
+// packed edge labels, with one L2 record load per matched edge. A chunk
 // that outgrows its lane is appended to the overflow queue as a CHUNK task, which the
 // persistent launch then runs with a whole warp. The kernel holds no per-warp shared
 // state and no warp-wide loop, so it runs in a separate, lighter launch than the
