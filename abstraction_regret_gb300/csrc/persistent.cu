@@ -5,9 +5,15 @@
 // calculator). Each warp pops tasks from a device queue with one atomicAdd ticket per
 // task, in the order the host gave them (longest first, so the longest serial chains
 // start first), until the queue is empty:
-//   - an NFA task (one input) is simulated by the whole warp with the automaton's own
-//     technique (dense bitmap or sparse list) from the device automaton table;
-//   - a DFA task (1..32 inputs of one DFA) runs one table walk per lane.
+//   - a WHOLE NFA task (one input) is simulated by the whole warp with the automaton's
+//     own technique (dense bitmap or sparse list) from the device automaton table;
+//   - a WHOLE DFA task (1..32 inputs of one DFA) runs one table walk per lane;
+//   - a CHUNK task runs one speculative chunk with the warp (run_chunk, chunks.cuh):
+//     chunks of automata that do not run in lanes, and lane chunks whose set outgrew
+//     the lane (the overflow queue);
+//   - a FIXUP task resolves one chunked input exactly from its chunk records
+//     (run_fixup, chunks.cuh).
+// LANES tasks belong to the lane launch (lanes.cu) and are skipped here.
 // Per-warp scratch: the dedup bitmap V and the two member lists in shared memory, sized
 // for the largest NFA of the launch; the dense buffers (D, FA, FB) in a global workspace
 // slice per resident warp. The reference has no counterpart: it launches one kernel per
