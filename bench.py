@@ -391,10 +391,22 @@ def main(argv=None) -> int:
 
             of, ol, oe = O.dfa_batch(b2.automata[0], b2.data, b2.offsets)
             assert np.array_equal(f2, of) and np.array_equal(l2, ol), f"DFA c2-{variant} parity"
+            examined_gbps = int(oe.sum()) / (d_ms * 1e-3) / 1e9
+            hbm_peak = float(json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+                             .get("hbm_gbs", 6800.0)) \
+                if (REPO / "MEASURED_PEAKS.json").exists() else 6800.0
+            # per examined symbol: 1 input byte (HBM stream) + one 2-byte table entry read
+            # from on-chip memory; each input is one chain of dependent lookups
+            longest = int(np.diff(b2.offsets).max())
             extras[f"dfa_c2_{variant}"] = {
                 "offered_GBps": b2.total_bytes / (d_ms * 1e-3) / 1e9,
-                "examined_GBps": int(oe.sum()) / (d_ms * 1e-3) / 1e9,
-                "ms": d_ms, "examined_bytes": int(oe.sum()), "checked": int(of.size)}
+                "examined_GBps": examined_gbps,
+                "ms": d_ms, "examined_bytes": int(oe.sum()), "checked": int(of.size),
+                "roofline": {"bound": "latency (one dependent lookup per symbol per input)",
+                             "hbm_frac_input_stream": examined_gbps / hbm_peak,
+                             "chains": int(b2.n_inputs),
+                             "ns_per_lookup_longest_chain": d_ms * 1e6 / max(1, longest)
+                             if variant == "sustained" else None}}
             del r2, ex2, b2
     if "c1" in sections and rank == 0:
         extras["c1_plain_nfa"] = c1_section(dev, max(2, args.steps // 2))
