@@ -242,7 +242,7 @@ class PersistentEngine:
             size += 64
         return int(min(size, 1 << 20))
 
-    def make_tasks(self, aut_ids, lengths, starts=None, lane_chunk: int | None = None,
+    def make_tasks(self, aut_ids, lengths, starts=None, lane_chunk=None,
                    warp_chunk: int | None = None) -> TaskPlan:
         """Task plan for a batch: input i is ``lengths[i]`` bytes at ``starts[i]`` (default:
         packed back to back from 0) on automaton ``aut_ids[i]``. Chunk bounds are nominal:
@@ -278,10 +278,17 @@ class PersistentEngine:
                 chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
             else:
                 chunk_w = warp_chunk or self.auto_chunk_bytes(int(lengths[warp_in].sum()))
-                chunk_l = lane_chunk or self.auto_lane_chunk_bytes(lengths[lane_in],
-                                                                   aut_ids[lane_in])
+                if isinstance(lane_chunk, np.ndarray):
+                    chunk_l = int(lane_chunk.max()) if lane_chunk.size else 0
+                else:
+                    chunk_l = lane_chunk or self.auto_lane_chunk_bytes(lengths[lane_in],
+                                                                       aut_ids[lane_in])
             csize[warp_in] = chunk_w
-            csize[lane_in] = chunk_l
+            if isinstance(lane_chunk, np.ndarray) and not self.chunk_bytes:
+                csize[lane_in] = np.maximum(np.asarray(lane_chunk, np.int64)[lane_in],
+                                            MIN_CHUNK)
+            else:
+                csize[lane_in] = chunk_l
         # every input of a lane automaton is chunked (a short one is a single exact
         # chunk); warp-chunked inputs are split when they span two chunks or more
         split = (csize > 0) & ((lengths >= 2 * np.maximum(csize, 1)) | lane_in)
@@ -383,14 +390,20 @@ class PersistentEngine:
         native.check(st, "gbfsm_persistent_run")
 
     def launch(self, d_data, d_off, dt: DeviceTasks, d_flags, d_lens, d_examined=None,
-               stream=None, d_ends=None, workspace=None, phases: dict | None = None) -> int:
+               stream=None, d_ends=None, workspace=None, phases: dict | None = None,
+               lane_slices=None) -> int:
         """Enqueue the batch's launches; returns how many kernels were launched:
         the lane launch (LANES tasks), the persistent launch (WHOLE / CHUNK tasks), the
         overflow pass (lane chunks that outgrew their lane, run by warps) and the fix-up
         (FIXUP tasks), each only when it has work. ``d_data`` is a device tensor or a raw
         device address (e.g. of pinned host memory read in place); with ``d_ends`` input
         i spans ``[d_off[i], d_ends[i])``. ``phases`` (optional) collects a pair of timing
-        events around each launch, keyed "lanes", "persistent", "overflow", "fixup"."""
+        events around each launch, keyed "lanes", "persistent", "overflow", "fixup".
+
+        ``lane_slices`` (optional) splits the lane launch: a list of ``(first task, task
+        count, side stream, event)``; each range of LANES tasks runs on its side stream
+        once the event (e.g. "its input bytes have arrived") has fired, and the rest of
+        the step waits for all of them, and for every event, on ``stream``."""
         stream = stream or torch.cuda.current_stream(self.device)
 
         def mark(name):
@@ -408,13 +421,37 @@ class PersistentEngine:
             with torch.cuda.stream(stream):
                 dt.d_overflow_count.zero_()
             io = dt.chunk_io()
-            mark("lanes")
-            st = native.lib().gbfsm_lanes_run(
-                self.table.data_ptr(), len(self.automata), base, dt.nl, data_ptr,
-                d_off.data_ptr(), ctypes.byref(io), stream.cuda_stream)
-            native.check(st, "gbfsm_lanes_run")
-            mark("lanes")
-            launches += 1
+            lib = native.lib()
+            if lane_slices:
+                fork = torch.cuda.Event()
+                fork.record(stream)
+                joins = []
+                for first, count, side, ready in lane_slices:
+                    if count <= 0:
+                        continue
+                    side.wait_event(fork)
+                    side.wait_event(ready)
+                    st = lib.gbfsm_lanes_run(
+                        self.table.data_ptr(), len(self.automata), base + int(first) * 16,
+                        int(count), data_ptr, d_off.data_ptr(), ctypes.byref(io),
+                        side.cuda_stream)
+                    native.check(st, "gbfsm_lanes_run")
+                    done = torch.cuda.Event()
+                    done.record(side)
+                    joins.append(done)
+                    launches += 1
+                for done in joins:
+                    stream.wait_event(done)
+                for _, _, _, ready in lane_slices:  # the launches below may read any slice
+                    stream.wait_event(ready)
+            else:
+                mark("lanes")
+                st = lib.gbfsm_lanes_run(
+                    self.table.data_ptr(), len(self.automata), base, dt.nl, data_ptr,
+                    d_off.data_ptr(), ctypes.byref(io), stream.cuda_stream)
+                native.check(st, "gbfsm_lanes_run")
+                mark("lanes")
+                launches += 1
         if dt.na or not (dt.nl or dt.nb):
             mark("persistent")
             self._run(base + dt.nl * 16, dt.na, dt, data_ptr, d_off, d_ends, d_flags, d_lens,
@@ -489,28 +526,6 @@ def slice_bounds(offsets: np.ndarray, parts: int) -> list[tuple[int, int]]:
     return [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
 
 
-class _Part:
-    """One slice of a pipelined batch: inputs [first, last), their task plan (the whole
-    batch's chunk sizes, the lane size scaled by `scale`), and a stream and workspace of
-    their own so that slices run concurrently."""
-
-    def __init__(self, engine, aut_ids, lengths, offsets, first, last, padded, whole,
-                 scale=1.0):
-        self.first, self.last = first, last
-        lane = int(whole.lane_chunk_bytes * scale) // 64 * 64
-        self.plan = engine.make_tasks(aut_ids[first:last], lengths[first:last],
-                                      starts=offsets[first:last],
-                                      lane_chunk=max(lane, MIN_CHUNK) if lane else None,
-                                      warp_chunk=whole.chunk_bytes or None)
-        self.tasks = DeviceTasks(engine.device)
-        self.lo = int(offsets[first]) // 16 * 16
-        self.hi = min(padded, -(-int(offsets[last]) // 16) * 16)
-        self.copied = torch.cuda.Event()
-        self.done = torch.cuda.Event()
-        self.stream = torch.cuda.Stream(engine.device)
-        self.workspace = engine.new_workspace()
-
-
 class GraphRunner:
     """A fixed batch captured as one CUDA graph: H2D inputs, the launches, D2H verdicts.
 
@@ -528,12 +543,13 @@ class GraphRunner:
         * ``copy``: one copy-engine transfer, then the launches;
         * ``zero_copy``: no copy, the simulation kernels read the bytes in place over the
           host link (NVLink-C2C on GB300);
-        * ``pipelined``: the batch is cut into ``parts`` slices of contiguous inputs with
-          about equal bytes, each with its own task plan and stream; a slice's launches
-          start as soon as its bytes have arrived, while later slices are still being
-          copied, and the slices run concurrently. Slice k of P uses the whole batch's
-          lane chunk size scaled by 1 - shrink * k / P: a slice that arrives later has
-          less time left, so its lanes get shorter chunks.
+        * ``pipelined``: the inputs are copied in ``parts`` slices of contiguous inputs
+          with about equal bytes. The lane tasks of each slice run on a stream of their
+          own as soon as the slice's bytes have arrived, concurrently with the copies of
+          later slices; the overflow pass and the fix-up then run once for the whole
+          batch. Inputs of slice k of P get the whole batch's lane chunk size scaled by
+          1 - shrink * k / P: a slice that arrives later has less time left, so its lanes
+          get shorter chunks.
 
         ``kernel_only`` always runs the whole-batch plan on the device copy."""
         if ingest not in self.INGEST:
@@ -546,6 +562,35 @@ class GraphRunner:
         lengths = np.diff(offsets)
         aut_ids = np.asarray(aut_ids)
         self.task_plan = engine.make_tasks(aut_ids, lengths)
+        self.slices: list[tuple[int, int, int, int]] = []  # (lo, hi, first task, count)
+        if ingest == "pipelined" and n:
+            spans = slice_bounds(offsets, parts)
+            base = self.task_plan.lane_chunk_bytes
+            sizes = np.zeros(n, np.int64)
+            for k, (a, b) in enumerate(spans):
+                sizes[a:b] = int(base * (1.0 - shrink * k / len(spans))) // 64 * 64
+            plan = engine.make_tasks(aut_ids, lengths, lane_chunk=sizes)
+            # a LANES task waits for the slice holding the last input it reads
+            firsts = np.asarray([a for a, _ in spans], np.int64)
+            ch_input = plan.chunks["input"].astype(np.int64)
+            tl = plan.tasks_l
+            if tl.shape[0]:
+                last_in = np.maximum.reduceat(ch_input[:plan.lane_chunks], tl[:, 1]) \
+                    if plan.lane_chunks else np.zeros(0, np.int64)
+                dep = np.searchsorted(firsts, last_in, side="right") - 1
+                order = np.argsort(dep, kind="stable")
+                plan.tasks_l = np.ascontiguousarray(tl[order])
+                counts = np.bincount(dep, minlength=len(spans))
+            else:
+                counts = np.zeros(len(spans), np.int64)
+            start = np.concatenate([[0], np.cumsum(counts)[:-1]])
+            total_b = max(16, -(-int(offsets[-1]) // 16) * 16)
+            for k, (a, b) in enumerate(spans):
+                self.slices.append((int(offsets[a]) // 16 * 16,
+                                    min(total_b, -(-int(offsets[b]) // 16) * 16),
+                                    int(start[k]), int(counts[k])))
+            self.pipe_plan = plan
+            self.pipe_tasks = DeviceTasks(dev)
         total = int(offsets[-1])
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
@@ -562,14 +607,11 @@ class GraphRunner:
         self.tasks = DeviceTasks(dev)
         self.with_examined = with_examined
         self.stream = torch.cuda.Stream(dev)
-        self.parts: list[_Part] = []
-        if ingest == "pipelined" and n:
-            spans = slice_bounds(offsets, parts)
-            self.parts = [_Part(engine, aut_ids, lengths, offsets, a, b, padded,
-                                self.task_plan, 1.0 - shrink * k / len(spans))
-                          for k, (a, b) in enumerate(spans)]
+        if self.slices:
             self.copy_stream = torch.cuda.Stream(dev)
-        plans = [q.plan for q in self.parts] or [self.task_plan]
+            self.slice_streams = [torch.cuda.Stream(dev) for _ in self.slices]
+            self.slice_events = [torch.cuda.Event() for _ in self.slices]
+        plans = [self.pipe_plan] if self.slices else [self.task_plan]
         self.h2d_bytes = padded + self.h_off.numel() * 8 + sum(
             (p.tasks_l.shape[0] + p.tasks_a.shape[0] + p.tasks_b.shape[0]) * 16
             + p.input_ids.size * 4 + p.chunks.shape[0] * 24 for p in plans)
@@ -591,27 +633,24 @@ class GraphRunner:
     def _body(self) -> None:
         s = torch.cuda.current_stream(self.engine.device)
         self.d_off.copy_(self.h_off, non_blocking=True)
-        if self.parts:
+        if self.slices:
             # the small task tables first, so they do not queue behind the input slices
-            for q in self.parts:
-                q.tasks.upload(q.plan, s)
+            self.pipe_tasks.upload(self.pipe_plan, s)
             start = torch.cuda.Event()
             start.record(s)
             self.copy_stream.wait_event(start)
             with torch.cuda.stream(self.copy_stream):
-                for q in self.parts:
-                    self.d_data[q.lo:q.hi].copy_(self.h_data[q.lo:q.hi], non_blocking=True)
-                    q.copied.record(self.copy_stream)
-            launches = 0
-            for q in self.parts:
-                q.stream.wait_event(q.copied)
-                f, l, ex = self._outputs(q.first)
-                launches += self.engine.launch(self.d_data, self.d_off[q.first:], q.tasks, f, l,
-                                               ex, q.stream, workspace=q.workspace)
-                q.done.record(q.stream)
-            for q in self.parts:
-                s.wait_event(q.done)
-            self.launches_per_step = launches
+                for (lo, hi, _, _), ev in zip(self.slices, self.slice_events):
+                    self.d_data[lo:hi].copy_(self.h_data[lo:hi], non_blocking=True)
+                    ev.record(self.copy_stream)
+            if not self.pipe_plan.tasks_l.shape[0]:
+                s.wait_stream(self.copy_stream)  # no lane launch to wait for the slices
+            f, l, ex = self._outputs(0)
+            lane_slices = [(first, count, side, ev) for (_, _, first, count), side, ev
+                           in zip(self.slices, self.slice_streams, self.slice_events)]
+            self.launches_per_step = self.engine.launch(self.d_data, self.d_off,
+                                                        self.pipe_tasks, f, l, ex, s,
+                                                        lane_slices=lane_slices)
         else:
             if self.ingest == "copy":
                 self.d_data.copy_(self.h_data, non_blocking=True)

@@ -326,9 +326,10 @@ def main(argv=None) -> int:
         "copy": "CUDA graph: inputs + tables H2D from pinned memory, launches, verdicts D2H",
         "zero_copy": "CUDA graph: tables H2D, kernels read the inputs from pinned host "
                      "memory over NVLink-C2C, verdicts D2H",
-        "pipelined": "CUDA graph: the batch in 8 slices copied H2D from pinned memory on "
-                     "a copy stream; each slice simulated on its own stream as soon as its "
-                     "bytes arrive (later slices with shorter lane chunks), verdicts D2H"}
+        "pipelined": "CUDA graph: the inputs copied H2D from pinned memory in 8 slices on "
+                     "a copy stream; each slice's lane tasks run on their own stream as "
+                     "soon as its bytes arrive (later slices with shorter lane chunks); "
+                     "overflow pass and fix-up once for the batch; verdicts D2H"}
     paths = {}
     for name, r in runners.items():
         with torch.cuda.stream(r.stream):

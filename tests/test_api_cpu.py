@@ -330,3 +330,15 @@ def test_pipeline_slices_are_contiguous_and_balanced():
     sizes = [off[b] - off[a] for a, b in spans]
     assert len(spans) == 8 and max(sizes) < 1.3 * off[-1] / 8
     assert slice_bounds(off[:2], 8) == [(0, 1)]
+
+
+def test_per_input_lane_chunk_sizes():
+    """The pipelined path gives later slices shorter lane chunks, per input."""
+    eng = _planner(["nfa"], [1], [1])
+    lengths = np.array([10000, 10000, 10000])
+    sizes = np.array([2048, 1024, 512])
+    p = eng.make_tasks(np.zeros(3, np.int64), lengths, lane_chunk=sizes)
+    for i, size in enumerate(sizes.tolist()):
+        c = p.chunks[p.chunks["input"] == i]
+        assert len(c) == -(-10000 // size)
+        assert (c["end"] - c["begin"]).max() <= size

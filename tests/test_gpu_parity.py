@@ -371,4 +371,5 @@ def test_graph_runner_ingest_paths(ingest):
         f, l, e = r.verdicts()
         assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
     if ingest == "pipelined":
-        assert len(r.parts) == 3
+        assert len(r.slices) == 3
+        assert sum(c for _, _, _, c in r.slices) == r.pipe_plan.tasks_l.shape[0]
