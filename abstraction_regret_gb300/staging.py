@@ -73,22 +73,6 @@ class Staging:
             self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
         return self._d_data[:padded], self._d_off[: n + 1], h_off, total
 
-    def put_flat(self, data: np.ndarray, offsets: np.ndarray, stream: torch.cuda.Stream):
-        """Like ``put`` for an already flat uint8 batch with int64 offsets."""
-        n = len(offsets) - 1
-        total = int(offsets[-1])
-        padded = max(PAD, -(-total // PAD) * PAD)
-        self._ensure(padded, n + 1)
-        h_off = self._h_off.numpy()[: n + 1]
-        h_off[:] = offsets
-        h_data = self._h_data.numpy()
-        h_data[:total] = data[:total]
-        h_data[total:padded] = 0
-        with torch.cuda.stream(stream):
-            self._d_data[:padded].copy_(self._h_data[:padded], non_blocking=True)
-            self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
-        return self._d_data[:padded], self._d_off[: n + 1], h_off, total
-
 
 class Results:
     """Device result arrays plus pinned host mirrors, reused across batches."""
