@@ -246,3 +246,43 @@ def test_protocol_on_live_walks_of_the_large_configuration():
         for chunk in (256, 1000):
             assert speculative(nfa, data, chunk) == want
             assert speculative(nfa, data, chunk, scan=True, even=True) == want
+
+
+def _true_sets(nfa, data):
+    """Active set after each prefix of data (index p: after p bytes), until it dies."""
+    cur = epsilon_closure({int(nfa.start_state)}, nfa)
+    out = [set(cur)]
+    for x in data:
+        cur = step(nfa, cur, x) if cur else set()
+        out.append(set(cur))
+    return out
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_two_byte_and_widened_start_sets_contain_the_true_set(seed):
+    """The lane start sets (csrc/chunks.cuh): the two-byte superset of x[b-2] x[b-1]
+    (pair_lanes), and the widened one -- the two-byte superset of x[b-4] x[b-3] stepped
+    over x[b-2] and x[b-1] -- both contain the true active set at b, for every b."""
+    from abstraction_regret_gb300.device import pair_lists
+
+    rng = random.Random(2000 + seed)
+    for _ in range(20):
+        nfa = _fuzz_nfa(rng, rng.randint(2, 60), "abcd", 0.02, 0.04, 0)  # no epsilon
+        first = first_lists(nfa)
+        pairs = pair_lists(nfa, first)
+        assert pairs is not None
+        prow, precs = pairs
+        data = bytes(ord(rng.choice("abcd")) for _ in range(rng.randint(8, 300)))
+        truth = _true_sets(nfa, data)
+
+        def pair_set(c1, c2):
+            k = c1 * 256 + c2
+            return {int(t) for t in precs[prow[k]:prow[k + 1], 0]}
+
+        for b in range(4, len(data) + 1):
+            two = pair_set(data[b - 2], data[b - 1])
+            assert truth[b] <= two
+            wide = pair_set(data[b - 4], data[b - 3])
+            for x in (data[b - 2], data[b - 1]):
+                wide = step(nfa, wide, x) if wide else set()
+            assert truth[b] <= wide <= two
