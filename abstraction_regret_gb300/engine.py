@@ -662,8 +662,9 @@ class GraphRunner:
         self.h_out.copy_(self.d_out, non_blocking=True)
 
     def replay(self) -> None:
-        """Launch the captured graph (asynchronous)."""
-        self.graph.replay()
+        """Launch the captured graph on the runner's stream (asynchronous)."""
+        with torch.cuda.stream(self.stream):
+            self.graph.replay()
 
     def kernel_only(self, stream=None, phases: dict | None = None) -> int:
         """The launches alone on resident inputs (for device-side timing)."""
@@ -675,5 +676,7 @@ class GraphRunner:
                                   phases=phases)
 
     def verdicts(self):
+        """(flags, lens, examined) of the last replay, once it has finished."""
+        self.stream.synchronize()
         h = self.h_out.numpy()
         return h[0, :self.n].copy(), h[1, :self.n].copy(), h[2, :self.n].copy()
