@@ -42,7 +42,7 @@ struct WarpScratch {
     uint64_t *V;   // [W] next-set bitmap; all-zero between steps
     uint64_t *D;   // [W] dense current set; all-zero while sparse
     uint64_t *FA;  // [W] dense closure frontier; all-zero between steps
-    uint64_t *FB;  // [W] dense closure frontier (next round); all-zero between steps
+    uint64_t *FB;  // [W] dense closure frontier (next closure pass); all-zero between steps
     uint4 *LA;     // [max(C, 32)] current member list
     uint4 *LB;     // [max(C, 32)] next member list (also the REG-mode compaction buffer)
     int C;         // list capacity; 0 = dense only
