@@ -111,6 +111,21 @@ def choose_nfa_plan(dev_nfa, n_inputs: int, persistent: bool = False):
     return rule_plan(f, n_inputs)
 
 
+# Longest input from which a batch goes to the chunked engine: a plain launch simulates
+# each input serially, one dependent L2 round trip (~0.5 us) or more per byte, so an
+# input of 512 bytes already costs it ~250 us, far more than the engine's few extra
+# launches; shorter batches are faster as one plain launch.
+ENGINE_MIN_LONGEST = 512
+
+
+def prefer_engine(dev_nfa, lengths) -> bool:
+    """Run this batch through the chunked engine rather than one plain launch?"""
+    lengths = np.asarray(lengths)
+    if lengths.size == 0 or not getattr(dev_nfa, "speculative", False):
+        return False
+    return int(lengths.max()) >= ENGINE_MIN_LONGEST
+
+
 def candidate_plans(f: Features) -> list[native.Plan]:
     """The plain-launch search space for one automaton."""
     out = []

@@ -104,6 +104,21 @@ gbfsm_plan plan_or_default(const gbfsm_plan *p, int32_t technique) {
     return q;
 }
 
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// The staged launches copy arrays into shared memory with cp.async.bulk, whose source
+// must be 16-byte aligned. A plan asking for staging of an NFA whose row or edge arrays
+// are not (e.g. views into a larger allocation) runs unstaged, reading them through L2;
+// the workspace query and the launch apply the same rule, so they agree.
+gbfsm_plan nfa_plan(const gbfsm_nfa_dev &a, const gbfsm_plan *plan) {
+    gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
+    const bool eps = (a.flags & GBFSM_NFA_HAS_EPS) != 0;
+    if (p.stage && !(aligned16(a.sym_row) && aligned16(a.sym_edges) &&
+                     (!eps || (aligned16(a.eps_row) && aligned16(a.eps_edges)))))
+        p.stage = 0;
+    return p;
+}
+
 }  // namespace
 }  // namespace gbfsm
 
@@ -154,7 +169,7 @@ gbfsm_status gbfsm_dfa_layout(int32_t num_states, const int32_t *trans, const ui
 size_t gbfsm_nfa_workspace_bytes(const gbfsm_nfa_dev *nfa, int32_t n_inputs,
                                  const gbfsm_plan *plan) {
     if (check_nfa(nfa) != GBFSM_OK || n_inputs <= 0) return 0;
-    const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
+    const gbfsm_plan p = nfa_plan(*nfa, plan);
     if (p.technique == GBFSM_TECH_BITMAP) {
         BitmapPlan bp;
         if (make_bitmap_plan(*nfa, n_inputs, p, bp) != GBFSM_OK || bp.sets_in_smem) return 0;
@@ -173,7 +188,7 @@ gbfsm_status gbfsm_nfa_run(const gbfsm_nfa_dev *nfa, const uint8_t *data, const 
     gbfsm_status st = check_nfa(nfa);
     if (st != GBFSM_OK) return st;
     if ((st = check_batch(data, offsets, n_inputs, flags, lens)) != GBFSM_OK) return st;
-    const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
+    const gbfsm_plan p = nfa_plan(*nfa, plan);
     const size_t need = gbfsm_nfa_workspace_bytes(nfa, n_inputs, &p);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GBFSM_INVALID_ARG, "workspace too small: %zu < %zu bytes", workspace_bytes,
@@ -211,7 +226,8 @@ gbfsm_status gbfsm_dfa_run(const gbfsm_dfa_dev *dfa, const uint8_t *data, const 
         return fail(GBFSM_INVALID_ARG, "2-byte entries hold at most 32768 states");
     gbfsm_status st = check_batch(data, offsets, n_inputs, flags, lens);
     if (st != GBFSM_OK) return st;
-    const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_DFA_WALK);
+    gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_DFA_WALK);
+    if (!aligned16(dfa->table)) p.stage = 0;  // cp.async.bulk needs an aligned source
     return launch_dfa_walk(*dfa, p, data, offsets, n_inputs, flags, lens, examined,
                            static_cast<cudaStream_t>(stream));
 }

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
     const int lane = (int)lane_id();
     if (lane >= task.count) return;
     const int cid = task.first + lane;
+    if (cid < 0 || cid >= io.n_chunks) return;  // a task naming chunks outside the table
     const gbfsm_chunk ch = io.chunks[cid];
     const int64_t off = offsets[ch.input];
     const gbfsm_automaton &T = table[task.automaton];
@@ -48,7 +49,10 @@ __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
         spill.first = cid;
         spill.count = 1;
         spill.kind = GBFSM_TASK_CHUNK;
-        io.overflow_tasks[atomicAdd(io.overflow_count, 1)] = spill;
+        // the queue holds n_chunks entries: only a task list naming a chunk twice could
+        // overflow it, and then the extra entries are dropped rather than written past it
+        const int slot = atomicAdd(io.overflow_count, 1);
+        if (slot < io.n_chunks) io.overflow_tasks[slot] = spill;
     }
 }
 

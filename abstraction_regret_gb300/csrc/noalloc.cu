@@ -6,7 +6,9 @@
 // first call on a device (with that device current) its address is looked up once with
 // cudaGetSymbolAddress and cached; every call then hands that address to the kernel as
 // its workspace. That first call is the set-up step: it loads the module and should come
-// before any stream capture on the device.
+// before any stream capture on the device. The cached address belongs to the device's
+// context: after a cudaDeviceReset of that device it is stale, so the entry point must
+// not be called again in that process.
 //
 // Nothing in the scratch has to start at zero: both kernels clear each warp's (or
 // thread's) slice of it before use, so no memset is issued.

@@ -104,6 +104,10 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
             R.eps_edges = nfa.eps_edges;
             S.C = (A->technique == GBFSM_TECH_WARP) ? 0 : min(A->list_capacity, L.C);
             if (task.kind == GBFSM_TASK_LANES) continue;  // gbfsm_lanes_run's tasks
+            // chunk tasks naming chunks outside the table are skipped
+            if ((task.kind == GBFSM_TASK_CHUNK || task.kind == GBFSM_TASK_FIXUP) &&
+                (task.first < 0 || task.count < 1 || task.first + task.count > io.n_chunks))
+                continue;
             if (task.kind == GBFSM_TASK_CHUNK) {
                 const gbfsm_chunk ch = chunks[task.first];
                 // a later chunk needs the one-byte supersets; without them it is not run

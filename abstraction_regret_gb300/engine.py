@@ -153,17 +153,24 @@ class PersistentEngine:
 
     def __init__(self, automata, device=None, choices=None, block_threads: int = 256,
                  list_capacity: int | None = None, ctas_per_sm: int = 0,
-                 chunk_bytes: int | None = 0, lane_pair_mean: float = LANE_PAIR_MEAN) -> None:
+                 chunk_bytes: int | None = 0, lane_pair_mean: float = LANE_PAIR_MEAN,
+                 resident=None) -> None:
         """``chunk_bytes``: 0 = chosen per batch, None = never chunk, else a fixed size.
-        ``lane_pair_mean``: largest mean two-byte superset for one-lane-per-chunk tasks."""
+        ``lane_pair_mean``: largest mean two-byte superset for one-lane-per-chunk tasks.
+        ``resident``: device layouts already built for ``automata`` (DeviceNFA /
+        DeviceDFA, same order), shared instead of built again."""
         self.device = resolve_device(device)
         self.automata = list(automata)
         if not self.automata:
             raise ValueError("the engine needs at least one automaton")
         self.kinds = [Kind.of(a) for a in self.automata]
-        self.dev = []
-        for a, k in zip(self.automata, self.kinds):
-            self.dev.append(DeviceNFA(a, self.device) if k is Kind.NFA else DeviceDFA(a, self.device))
+        if resident is not None:
+            self.dev = list(resident)
+            if len(self.dev) != len(self.automata):
+                raise ValueError("one resident layout per automaton is needed")
+        else:
+            self.dev = [DeviceNFA(a, self.device) if k is Kind.NFA else DeviceDFA(a, self.device)
+                        for a, k in zip(self.automata, self.kinds)]
         choices = list(choices) if choices is not None else [NfaChoice() for _ in self.automata]
         self.choices = choices
         self.chunk_bytes = chunk_bytes
@@ -585,10 +592,14 @@ class GraphRunner:
                 counts = np.zeros(len(spans), np.int64)
             start = np.concatenate([[0], np.cumsum(counts)[:-1]])
             total_b = max(16, -(-int(offsets[-1]) // 16) * 16)
+            # slice k ends at the 16-byte block holding its last input's end and the next
+            # slice starts there, so no block is copied twice (a block shared by two inputs
+            # arrives with the earlier slice, which the later slice's copy follows)
+            lo = 0
             for k, (a, b) in enumerate(spans):
-                self.slices.append((int(offsets[a]) // 16 * 16,
-                                    min(total_b, -(-int(offsets[b]) // 16) * 16),
-                                    int(start[k]), int(counts[k])))
+                hi = min(total_b, -(-int(offsets[b]) // 16) * 16)
+                self.slices.append((lo, hi, int(start[k]), int(counts[k])))
+                lo = hi
             self.pipe_plan = plan
             self.pipe_tasks = DeviceTasks(dev)
         total = int(offsets[-1])

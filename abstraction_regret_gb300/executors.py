@@ -12,7 +12,9 @@ reference's own GPU tests keep working, each mapped onto this engine's kernels:
 ====================  ===========================================================
 NFA name              engine kernel
 ====================  ===========================================================
-auto (default)        autotuned: bitmap / warp / compact, block shape, staging
+auto (default)        per batch: the persistent engine (chunked, see below) when
+                      inputs are long enough to cut, else the autotuned plain
+                      launch (bitmap / warp / compact, block shape, staging)
 bitmap, worklist,     thread per input, packed bitmap in shared memory
 multistream, dense,   (``worklist`` and ``multistream_shared`` stage the edge rows
 bitpacked,            in shared memory with TMA bulk copies; ``multistream_async``
@@ -41,7 +43,7 @@ import numpy as np
 import torch
 
 from . import native
-from .autotune import choose_nfa_plan
+from .autotune import choose_nfa_plan, prefer_engine
 from .device import DeviceDFA, DeviceNFA, resolve_device
 from .engine import NfaChoice, PersistentEngine
 from .registry import Backend, Kind, register, register_availability, set_unavailable_reason
@@ -197,13 +199,15 @@ class CudaDFAExecutor(_BatchExecutor):
 class CudaPersistentExecutor:
     """A single automaton run through the persistent batched engine."""
 
-    def __init__(self, automaton, technique: str = "persistent", device=None) -> None:
+    def __init__(self, automaton, technique: str = "persistent", device=None,
+                 resident=None) -> None:
         self.automaton = automaton
         self.technique = technique
         choice = NfaChoice()
         if Kind.of(automaton) is Kind.NFA:
             choice = choose_nfa_plan(automaton, 0, persistent=True)
-        self.engine = PersistentEngine([automaton], device, choices=[choice])
+        self.engine = PersistentEngine([automaton], device, choices=[choice],
+                                       resident=[resident] if resident is not None else None)
 
     def run_arrays(self, inputs, with_examined: bool = False):
         _check_inputs(inputs)
@@ -218,6 +222,52 @@ class CudaPersistentExecutor:
 
     def run(self, input_bytes: bytes) -> Result:
         return self.run_batch([input_bytes])[0]
+
+
+class CudaAutoNFAExecutor:
+    """The default NFA technique: per batch, one plain launch or the chunked engine.
+
+    A plain launch simulates each input serially (one warp per input), so its time grows
+    with the longest input; the engine cuts long inputs into chunks that run in parallel
+    and resolves them exactly, at the cost of a few more launches. ``prefer_engine``
+    (autotune.py) makes the choice from the automaton's features and the batch's lengths;
+    both paths share one resident device layout."""
+
+    def __init__(self, nfa, device=None) -> None:
+        self.nfa = nfa
+        self.technique = "auto"
+        self.plain = CudaNFAExecutor(nfa, "auto", device)
+        self.device = self.plain.device
+        self._engine: CudaPersistentExecutor | None = None
+        self.last_path = None
+
+    def engine(self) -> CudaPersistentExecutor:
+        if self._engine is None:
+            self._engine = CudaPersistentExecutor(self.nfa, "persistent", self.device,
+                                                  resident=self.plain.dev)
+        return self._engine
+
+    def run_arrays(self, inputs, with_examined: bool = False):
+        _check_inputs(inputs)
+        lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=len(inputs))
+        if prefer_engine(self.plain.dev, lengths):
+            self.last_path = "engine"
+            return self.engine().run_arrays(inputs, with_examined)
+        self.last_path = "plain"
+        return self.plain.run_arrays(inputs, with_examined)
+
+    def run_batch(self, inputs) -> list[Result]:
+        if not inputs:
+            return []
+        flags, lens, _, kms, tms = self.run_arrays(inputs)
+        return batch_results(flags, lens, kms, tms)
+
+    def run(self, input_bytes: bytes) -> Result:
+        return self.run_batch([input_bytes])[0]
+
+    def launch(self, d_data, d_off, n, d_flags, d_lens, d_examined=None, stream=None) -> None:
+        """One plain launch on resident device buffers (no synchronisation)."""
+        self.plain.launch(d_data, d_off, n, d_flags, d_lens, d_examined, stream)
 
 
 # ---- executor cache -------------------------------------------------------------------
@@ -259,6 +309,8 @@ def make_nfa_executor(automaton, technique: str):
         raise TypeError("an NFA technique was asked to run a DFA")
     if technique == "persistent":
         return _cached(automaton, technique, lambda: CudaPersistentExecutor(automaton, technique))
+    if technique == "auto":
+        return _cached(automaton, technique, lambda: CudaAutoNFAExecutor(automaton))
     return _cached(automaton, technique, lambda: CudaNFAExecutor(automaton, technique))
 
 

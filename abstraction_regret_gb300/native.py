@@ -175,6 +175,10 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_nfa_run_static": (ctypes.c_int, [_P(NfaDev), _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                             _vp, _vp]),
     "gbfsm_workload_walk": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _u64, _vp, _i32]),
+    "gbfsm_probe_l2_read": (ctypes.c_int, [_vp, _sz, _i32, _vp, _vp]),
+    "gbfsm_probe_gather16": (ctypes.c_int, [_vp, _sz, _i64, _i32, _vp, _vp]),
+    "gbfsm_probe_chase": (ctypes.c_int, [_vp, ctypes.c_uint32, _i64, _i32, _vp, _vp]),
+    "gbfsm_probe_smem": (ctypes.c_int, [_i64, _i32, _vp, _vp]),
 }
 
 ABI_VERSION = 1

@@ -154,8 +154,12 @@ def walk_bytes(nfa, offsets: np.ndarray, seed: int, threads: int | None = None) 
 # ---- configurations ------------------------------------------------------------------------
 
 
-def c1(variant: str = "literal", check=None, max_tries: int = 64) -> Batch:
-    """Plain NFA. ``check(nfa, data, offsets) -> bool[n]`` applies the divergence rule."""
+def c1(variant: str = "literal", check=None, max_tries: int = 64, walk=None) -> Batch:
+    """Plain NFA. ``check(nfa, data, offsets) -> bool[n]`` applies the divergence rule.
+    ``walk`` generates the random-walk inputs (default ``walk_bytes``; any generator
+    giving the same bytes, e.g. a CPU-only one for a process that must not load the
+    library)."""
+    walk = walk or walk_bytes
     nfa = random_nfa(1024, seed=0, degree=2, accept_prob=0.01)
     n, length = 64, 4096
     offsets = offsets_of(np.full(n, length, dtype=np.int64))
@@ -175,7 +179,7 @@ def c1(variant: str = "literal", check=None, max_tries: int = 64) -> Batch:
             meta.update(regen_tries=tries, regen_satisfied=int(ok.sum()))
     else:
         a = nfa if variant == "live" else without_accepts(nfa)
-        data = walk_bytes(nfa, offsets, seed=10)
+        data = walk(nfa, offsets, seed=10)
         nfa = a
     return Batch("c1-" + variant, [nfa], np.zeros(n, np.int64), data, offsets, meta)
 
@@ -191,15 +195,17 @@ def c2(variant: str = "literal", n_inputs: int = 4096, length: int = 65536) -> B
     return Batch("c2-" + variant, [dfa], np.zeros(n_inputs, np.int64), data, offsets, meta)
 
 
-def c3(variant: str = "literal", n_inputs: int = 2048) -> Batch:
-    """Batched NFA with uneven inputs (16384 states, Poisson(4) degree, 0.1% accepting)."""
+def c3(variant: str = "literal", n_inputs: int = 2048, walk=None) -> Batch:
+    """Batched NFA with uneven inputs (16384 states, Poisson(4) degree, 0.1% accepting).
+    ``walk`` as for ``c1``."""
+    walk = walk or walk_bytes
     nfa = random_nfa(16384, seed=2, poisson=4.0, accept_prob=0.001)
     lengths = log_uniform_lengths(np.random.default_rng([2, 1]), n_inputs, 256, 1 << 20)
     offsets = offsets_of(lengths)
     if variant == "literal":
         data = uniform_bytes([2, 2], int(offsets[-1]))
     else:
-        data = walk_bytes(nfa, offsets, seed=20)
+        data = walk(nfa, offsets, seed=20)
         if variant == "sustained":
             nfa = without_accepts(nfa)
     meta = {"config": "c3", "variant": variant, "states": 16384, "inputs": n_inputs}
@@ -212,8 +218,10 @@ def c4_automaton(seed: int) -> NFA:
     return random_nfa(n, seed=seed, degree=(1, 8), accept_prob=0.01)
 
 
-def c4(variant: str = "literal", per_automaton: int = 16) -> Batch:
-    """64 NFAs (seeds 100..163), 16 inputs each, all in one persistent launch."""
+def c4(variant: str = "literal", per_automaton: int = 16, walk=None) -> Batch:
+    """64 NFAs (seeds 100..163), 16 inputs each, all in one persistent launch. ``walk``
+    as for ``c1``."""
+    walk = walk or walk_bytes
     automata, lens, ids = [], [], []
     for k, seed in enumerate(range(100, 164)):
         automata.append(c4_automaton(seed))
@@ -230,7 +238,7 @@ def c4(variant: str = "literal", per_automaton: int = 16) -> Batch:
         for k, a in enumerate(automata):
             sel = np.flatnonzero(aut_ids == k)
             sub = offsets_of(lengths[sel])
-            chunk = walk_bytes(a, sub, seed=1000 + k)
+            chunk = walk(a, sub, seed=1000 + k)
             data[offsets[sel[0]]:offsets[sel[-1] + 1]] = chunk
         if variant == "sustained":
             automata = [without_accepts(a) for a in automata]

@@ -64,7 +64,7 @@ def parse_args(argv=None):
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline measurement (used for profiling)")
-    ap.add_argument("--extras", default="plain,c1,dfa,c4,serving",
+    ap.add_argument("--extras", default="plain,run_batch,c1,dfa,c4,serving",
                     help="comma-separated extra sections after the headline")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the c5 serving trace (0: skip the serving section)")
@@ -80,11 +80,24 @@ def dist_env():
     return world, rank, local
 
 
-def load_workload(name: str):
+def load_workload(name: str, reference_arm: bool = False):
+    """The named batch. The CPU reference arm generates its random-walk inputs with the
+    oracle's walker (byte-identical), so that it loads no product library."""
     from abstraction_regret_gb300 import workloads as W
 
-    variant = name.split("-", 1)[1]
-    return W.c3(variant)
+    config, variant = name.split("-", 1)
+    walk = None
+    if reference_arm:
+        from oracle import oracle as O
+
+        walk = O.walk_bytes
+    return {"c1": W.c1, "c3": W.c3}[config](variant, walk=walk)
+
+
+def workload_config(workload: str) -> str:
+    """The workload string both arms print (same configuration, same words)."""
+    return (f"{workload}: 16384-state NFA, Poisson(4) degree, 0.1% accepting (cleared when "
+            "sustained), 2048 inputs log-uniform 256 B..1 MiB")
 
 
 # ---- clocks during the timed region -------------------------------------------------------
@@ -95,8 +108,9 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int) -> None:
+    def __init__(self, gpu_index: int, period_ms: int = 20) -> None:
         self.gpu = gpu_index
+        self.period_ms = period_ms
         self.proc = None
         self.path = None
 
@@ -106,10 +120,21 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        # wait (bounded) for the first sample, so the timed region that follows is covered
+        t0 = time.monotonic()
+        while self.proc is not None and time.monotonic() - t0 < 5.0:
+            if self.proc.poll() is not None:
+                break
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):
@@ -212,7 +237,7 @@ def run_reference(args, world, rank):
     """--impl reference: the reference algorithm (C port of the oracle) on host cores."""
     if rank != 0:
         return 0
-    batch = load_workload(args.workload)
+    batch = load_workload(args.workload, reference_arm=True)
     samples = []
     info = None
     for i in range(args.warmup + args.steps):
@@ -225,8 +250,7 @@ def run_reference(args, world, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: 16384-state NFA, Poisson(4) degree, "
-                                   "2048 inputs log-uniform 256 B..1 MiB",
+            "config": {"workload": workload_config(args.workload),
                        "sample": info["sample"]},
             "cpu_baseline": info,
             "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -300,20 +324,21 @@ def main(argv=None) -> int:
         for _ in range(args.warmup):
             runner.kernel_only(stream)
     phases: dict = {}
+    # clocks are sampled over the headline's and the e2e paths' timed regions
+    clk = ClockSampler(local).__enter__()
     barrier()
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-            launches = 0
-            for _ in range(args.steps):
-                launches += runner.kernel_only(stream, phases=phases)
-            e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        torch.cuda.synchronize()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        launches = 0
+        for _ in range(args.steps):
+            launches += runner.kernel_only(stream, phases=phases)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    torch.cuda.synchronize()
     barrier()
     ms = max_over_ranks(ms, dev, world)
     value = replica_throughput(offered, ms, world)
@@ -339,6 +364,7 @@ def main(argv=None) -> int:
                        "h2d_bytes_per_step": int(r.h2d_bytes),
                        "d2h_bytes_per_step": int(r.d2h_bytes), "ms_per_step": e2e_ms,
                        "path": describe[name]}
+    clk.__exit__(None, None, None)
     best = max(paths, key=lambda k: paths[k]["value"])
     e2e = paths[best]
     e2e_other = {k: v for k, v in paths.items() if k != best}
@@ -409,6 +435,8 @@ def main(argv=None) -> int:
                              "ns_per_lookup_longest_chain": d_ms * 1e6 / max(1, longest)
                              if variant == "sustained" else None}}
             del r2, ex2, b2
+    if "run_batch" in sections and rank == 0:
+        extras["run_batch_default"] = run_batch_section(batch, flags, lens, steps=3)
     if "c1" in sections and rank == 0:
         extras["c1_plain_nfa"] = c1_section(dev, max(2, args.steps // 2))
     if "c4" in sections and rank == 0:
@@ -417,6 +445,11 @@ def main(argv=None) -> int:
         extras["serving"] = serving_section(dev, args.serve_requests, args.slo_ms)
 
     cpu = cpu_reference(batch) if rank == 0 else None
+    onchip = None
+    if rank == 0:
+        from abstraction_regret_gb300 import peaks as P
+
+        onchip = P.measure(dev)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     peaks = {}
@@ -442,24 +475,40 @@ def main(argv=None) -> int:
             parts = line.split()
             if len(parts) == 3 and parts[0] == kernel_name and parts[1] == args.workload:
                 traffic = int(parts[2])
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic,
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+    # the bound: the edge gathers are served on chip (a 1 MiB record table), so the
+    # algorithmic bytes are held against the L2 read bandwidth measured in this run; the
+    # input stream alone against HBM; and a latency bound: every lane chain waits for one
+    # dependent L2 record load per byte, so at most chains / L2 latency symbols per second
+    l2 = onchip.get("l2_read_GBps") if onchip else None
+    chains = min(int(runner.task_plan.lane_chunks),
+                 eng.sm_count * eng.lane_warps_per_sm * 32) if runner.task_plan.lane_chunks else 0
+    lat_ns = onchip.get("l2_latency_ns") if onchip else None
+    symbols = gate.get("examined_bytes", examined_bytes)
+    roofline = {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
+                "frac": achieved / l2 if l2 else None, "traffic": traffic,
+                "peak_source": "measured in this run: L2 streaming read (gbfsm_probe_l2_read)",
                 "kernel": kernel_name, "kernel_ms": kernel_ms,
                 "algorithmic_bytes_per_launch": int(algo),
                 "input_stream": {"achieved": examined_bytes / (kernel_ms * 1e-3) / 1e9,
-                                 "frac": examined_bytes / (kernel_ms * 1e-3) / 1e9 / hbm},
-                "note": "algorithmic bytes are mostly edge gathers served by L1/L2 (see "
-                        "profiles/lanes_kernel_c3-sustained.md); DRAM carries the input"}
+                                 "peak": hbm, "frac": examined_bytes / (kernel_ms * 1e-3) / 1e9 / hbm,
+                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"
+                                 if "hbm_gbs" in peaks else "fallback"},
+                "latency": {"chains": chains, "l2_latency_ns": lat_ns,
+                            "bound_Gsymbols_per_s": chains / lat_ns if chains and lat_ns else None,
+                            "achieved_Gsymbols_per_s": symbols / (kernel_ms * 1e-3) / 1e9,
+                            "frac": (symbols / (kernel_ms * 1e-3) / 1e9) / (chains / lat_ns)
+                            if chains and lat_ns else None},
+                "onchip_peaks": onchip,
+                "note": "algorithmic bytes (per symbol: 1 input byte, 8 per active state, 8 "
+                        "per scanned edge) are mostly edge gathers from a 1 MiB table held "
+                        "in L1/L2; DRAM carries the input stream"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "u8", "data": "synthetic (seeded; random-walk inputs for live/sustained)",
-                "config": {"workload": f"{args.workload}: 16384-state NFA, Poisson(4) degree, "
-                                       "0.1% accepting (cleared when sustained), 2048 inputs "
-                                       "log-uniform 256 B..1 MiB",
+                "config": {"workload": workload_config(args.workload),
                            "offered_bytes": offered, "examined_bytes": examined_bytes,
                            "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}",
@@ -476,6 +525,33 @@ def main(argv=None) -> int:
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def run_batch_section(batch, flags, lens, steps: int = 3) -> dict:
+    """The drop-in call with host bytes: ``run_batch(nfa, inputs)`` with the default
+    technique (what ``gpufsm.run_batch(nfa, inputs, backend="cuda")`` runs once the plugin
+    is installed), wall-clock per call: packing the bytes into pinned memory, planning,
+    the copies, the launches and the verdicts back."""
+    import abstraction_regret_gb300 as G
+    from abstraction_regret_gb300.executors import make_nfa_executor
+
+    nfa = batch.automata[0]
+    inputs = batch.inputs()
+    res = G.run_batch(nfa, inputs)  # warm-up (executor build, buffers)
+    got_f = np.fromiter((r.accepted for r in res), dtype=np.int32, count=len(res))
+    got_l = np.fromiter((r.match_len for r in res), dtype=np.int32, count=len(res))
+    if not (np.array_equal(got_f, flags) and np.array_equal(got_l, lens)):
+        raise SystemExit("run_batch default technique differs from the gated verdicts")
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        G.run_batch(nfa, inputs)
+        times.append(time.perf_counter() - t0)
+    ms = float(np.median(times)) * 1e3
+    path = make_nfa_executor(nfa, "auto").last_path
+    return {"value": batch.total_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "ms": ms,
+            "calls": steps, "path": path, "kernel_ms_result0": float(res[0].kernel_ms),
+            "note": "wall clock per call (median), host bytes in, verdicts out"}
 
 
 def c1_section(dev, steps: int) -> dict:

@@ -146,7 +146,12 @@ typedef struct gbfsm_plan {
     int32_t technique;     /* GBFSM_TECH_* */
     int32_t block_threads; /* threads per CTA (multiple of 32) */
     int32_t list_capacity; /* sparse active-list capacity per warp (COMPACT) */
-    int32_t stage;         /* 1: stage edges / DFA table in shared memory when they fit */
+    int32_t stage;         /* 1: stage edges / DFA table in shared memory when they fit.
+                              Staging copies sym_row, sym_edges, eps_row, eps_edges (or
+                              the DFA table) with bulk copies of whole 16-byte blocks: it
+                              is used only when each of them starts 16-byte aligned (else
+                              the launch reads them through L2), and each must then be
+                              readable up to the next 16-byte boundary past its end. */
     int32_t ctas_per_sm;   /* persistent launches: CTAs per SM (0 = from occupancy) */
     int32_t reserved[3];
 } gbfsm_plan;
@@ -222,10 +227,12 @@ gbfsm_status gbfsm_nfa_run(const gbfsm_nfa_dev *nfa, const uint8_t *data,
  * an allocator while requests are in flight. Returns GBFSM_INVALID_ARG, writing
  * nothing, when the batch needs more scratch than that (gbfsm_nfa_workspace_bytes of
  * the same arguments). The first call on a device looks up the array's address
- * (module load); make it before any stream capture. All calls on a device share the
- * one array: calls whose kernels overlap on the GPU race on it and must be ordered
- * (e.g. issued on one stream). Results are those of gbfsm_nfa_run. No counterpart in
- * the reference. */
+ * (module load); make it before any stream capture. The address is kept for the life
+ * of the process and is valid only as long as the device's context: after
+ * cudaDeviceReset on that device, do not call this entry point again in the same
+ * process. All calls on a device share the one array: calls whose kernels overlap on the
+ * GPU race on it and must be ordered (e.g. issued on one stream). Results are those of
+ * gbfsm_nfa_run. No counterpart in the reference. */
 gbfsm_status gbfsm_nfa_run_static(const gbfsm_nfa_dev *nfa, const uint8_t *data,
                                   const int64_t *offsets, int32_t n_inputs,
                                   const gbfsm_plan *plan, int32_t *flags, int32_t *lens,
@@ -419,6 +426,34 @@ gbfsm_status gbfsm_run_dfa_bytes(const int32_t *trans, const uint8_t *accept, in
                                  int32_t start_state, const uint8_t *data, const int64_t *offsets,
                                  int32_t num_strings, const gbfsm_plan *plan, int32_t *out_flags,
                                  int32_t *out_lens, float *kernel_ms);
+
+/* ---------------------------------------------------------------------------------
+ * On-chip peak probes (no counterpart in the reference, whose rooflines use nominal
+ * DRAM figures). The simulation kernels read edge records and DFA tables that stay in
+ * L1/L2/shared memory, so their rooflines need measured L2 and shared-memory figures.
+ * Each call enqueues one launch on `stream`; the caller times it with events. Buffers
+ * are device buffers owned by the caller; `sink` is a device uint64 that a launch
+ * writes only when its checksum equals a fixed constant (it keeps the loads alive).
+ * ------------------------------------------------------------------------------- */
+
+/* `passes` passes of 16-byte L2-only loads (ld.global.cg) over `bytes` of `buf` (16-byte
+ * aligned) by 8 CTAs of 256 threads per SM: bytes * passes read. */
+gbfsm_status gbfsm_probe_l2_read(const void *buf, size_t bytes, int32_t passes, uint64_t *sink,
+                                 void *stream);
+/* Independent 16-byte loads at pseudo-random entries of `table` (a power-of-two number of
+ * 16-byte entries, 16-byte aligned): 8 CTAs of 256 threads per SM, each making
+ * loads_per_thread rounded up to a multiple of 8 loads; via_l1 = 0 reads through L2
+ * only, 1 through L1 (ld.global.nc). */
+gbfsm_status gbfsm_probe_gather16(const void *table, size_t table_bytes, int64_t loads_per_thread,
+                                  int32_t via_l1, uint64_t *sink, void *stream);
+/* `chains` threads of one CTA each follow p = next[p] & (n - 1) for `steps` dependent
+ * L2-only 4-byte loads (n a power of two): the duration / steps is the latency of one
+ * dependent load. */
+gbfsm_status gbfsm_probe_chase(const uint32_t *next, uint32_t n, int64_t steps, int32_t chains,
+                               uint64_t *sink, void *stream);
+/* blocks_per_sm (1..8) CTAs of 256 threads per SM, each thread making `iters` 16-byte
+ * bank-conflict-free shared-memory loads: 4096 * iters bytes per CTA. */
+gbfsm_status gbfsm_probe_smem(int64_t iters, int32_t blocks_per_sm, uint64_t *sink, void *stream);
 
 /* ---------------------------------------------------------------------------------
  * Synthetic workload generator (host only; no counterpart in the reference, which

@@ -314,4 +314,189 @@ int fsm_oracle_dfa_batch(int32_t num_states, int32_t start_state, const uint8_t 
     return run_pool(&job, n_threads, dfa_worker);
 }
 
+/* ---- random-walk input generator for the CPU reference arm ------------------------------
+ *
+ * The benchmark's "live" and "sustained" inputs are random walks through an automaton's
+ * live core; the product library generates them for the GPU arm. The CPU reference arm
+ * must not load the product library, so it generates the same bytes here. The walk:
+ *   - live core = the largest set of non-accepting states in which every state has a
+ *     symbol edge to another state of the set (prune states without such an edge until
+ *     nothing changes);
+ *   - input i uses a SplitMix64 stream (Steele, Lea & Flood, OOPSLA 2014) seeded with
+ *     seed * 0x100000001b3 ^ (i + 1) * 0x9e3779b97f4a7c15; at each position the walk
+ *     state draws one of its edges into the core uniformly (multiply-shift of the top 32
+ *     bits), emits the edge's symbol (a draw's low byte for ANY) and moves on;
+ *   - once the walk is outside the core (or the core gives no edge), the rest of the
+ *     input is the low bytes of successive draws.
+ * tests/test_oracle.py checks that both generators give identical bytes. */
+
+typedef struct {
+    uint64_t s;
+} mix_t;
+
+static uint64_t mix_next(mix_t *r) {
+    uint64_t z = (r->s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+static uint32_t mix_below(mix_t *r, uint32_t n) {
+    return (uint32_t)(((mix_next(r) >> 32) * (uint64_t)n) >> 32);
+}
+
+/* live[s] = 1 for the states of the live core; returns -2 on allocation failure. */
+static int live_states(int32_t n, const int32_t *srp, const int32_t *stg, const uint8_t *accept,
+                       uint8_t *live) {
+    const int32_t nnz = srp[n];
+    int32_t *deg = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *rrow = (int32_t *)calloc((size_t)n + 1, sizeof(int32_t));
+    int32_t *pos = (int32_t *)malloc(sizeof(int32_t) * ((size_t)n + 1));
+    int32_t *rsrc = (int32_t *)malloc(sizeof(int32_t) * ((size_t)nnz + 1));
+    int32_t *queue = (int32_t *)malloc(sizeof(int32_t) * ((size_t)n + 1));
+    int rc = 0;
+    if (!deg || !rrow || !pos || !rsrc || !queue) {
+        rc = -2;
+        goto out;
+    }
+    /* reverse edges, and each state's count of edges into non-accepting states */
+    for (int32_t k = 0; k < nnz; ++k)
+        if (stg[k] >= 0 && stg[k] < n) rrow[stg[k] + 1]++;
+    for (int32_t s = 0; s < n; ++s) rrow[s + 1] += rrow[s];
+    memcpy(pos, rrow, sizeof(int32_t) * (size_t)n);
+    for (int32_t s = 0; s < n; ++s) {
+        for (int32_t k = srp[s]; k < srp[s + 1]; ++k) {
+            const int32_t t = stg[k];
+            if (t < 0 || t >= n) continue;
+            rsrc[pos[t]++] = s;
+            if (!accept[t]) deg[s]++;
+        }
+    }
+    int32_t qn = 0;
+    for (int32_t s = 0; s < n; ++s) {
+        live[s] = (uint8_t)!(accept[s] || deg[s] == 0);
+        if (!live[s]) queue[qn++] = s;
+    }
+    for (int32_t q = 0; q < qn; ++q) {
+        const int32_t t = queue[q];
+        if (accept[t]) continue; /* its in-edges were never counted */
+        for (int32_t r = rrow[t]; r < rrow[t + 1]; ++r) {
+            const int32_t s = rsrc[r];
+            if (live[s] && --deg[s] == 0) {
+                live[s] = 0;
+                queue[qn++] = s;
+            }
+        }
+    }
+out:
+    free(deg);
+    free(rrow);
+    free(pos);
+    free(rsrc);
+    free(queue);
+    return rc;
+}
+
+typedef struct {
+    int32_t n, start;
+    const int32_t *srp, *stg, *ssy;
+    const uint8_t *live;
+    const int64_t *offsets;
+    int64_t n_inputs;
+    uint64_t seed;
+    uint8_t *out;
+    int32_t stride;
+    int32_t next_worker;
+    int32_t max_degree;
+    int32_t failed;
+    pthread_mutex_t mu;
+} walk_job_t;
+
+static void walk_one_input(const walk_job_t *job, int64_t i, int32_t *good) {
+    mix_t r = {job->seed * 0x100000001b3ull ^ (uint64_t)(i + 1) * 0x9e3779b97f4a7c15ull};
+    uint8_t *o = job->out + job->offsets[i];
+    const int64_t len = job->offsets[i + 1] - job->offsets[i];
+    int32_t s = job->start;
+    int64_t p = 0;
+    for (; p < len && job->live[s]; ++p) {
+        int32_t ng = 0;
+        for (int32_t k = job->srp[s]; k < job->srp[s + 1]; ++k) {
+            const int32_t t = job->stg[k];
+            if (t >= 0 && t < job->n && job->live[t]) good[ng++] = k;
+        }
+        if (ng == 0) break;
+        const int32_t k = good[mix_below(&r, (uint32_t)ng)];
+        const int32_t sym = job->ssy[k];
+        o[p] = (sym >= 0 && sym <= 255) ? (uint8_t)sym : (uint8_t)(mix_next(&r) & 0xffu);
+        s = job->stg[k];
+    }
+    for (; p < len; ++p) o[p] = (uint8_t)(mix_next(&r) & 0xffu);
+}
+
+/* Each call claims stripes (inputs me, me + stride, ...) until none is left, so every
+ * stripe is generated once whether or not all threads could be started. */
+static void *walk_worker(void *arg) {
+    walk_job_t *job = (walk_job_t *)arg;
+    int32_t *good = (int32_t *)malloc(sizeof(int32_t) * ((size_t)job->max_degree + 1));
+    for (;;) {
+        pthread_mutex_lock(&job->mu);
+        const int32_t me = job->next_worker++;
+        if (!good) job->failed = 1;
+        pthread_mutex_unlock(&job->mu);
+        if (me >= job->stride || !good) break;
+        for (int64_t i = me; i < job->n_inputs; i += job->stride) walk_one_input(job, i, good);
+    }
+    free(good);
+    return NULL;
+}
+
+/* Random-walk inputs: out[offsets[i] .. offsets[i+1]) for every input i (see above).
+ * Returns 0, -1 for invalid arguments, -2 on allocation failure. */
+int fsm_oracle_walk(int32_t num_states, const int32_t *sym_row_ptr, const int32_t *sym_targets,
+                    const int32_t *sym_symbols, const uint8_t *accept, int32_t start_state,
+                    const int64_t *offsets, int64_t n_inputs, uint64_t seed, uint8_t *out,
+                    int32_t n_threads) {
+    if (num_states < 1 || start_state < 0 || start_state >= num_states || n_inputs < 0 ||
+        !sym_row_ptr || !accept || !offsets || !out || offsets_valid(offsets, n_inputs) != 0)
+        return -1;
+    uint8_t *live = (uint8_t *)malloc((size_t)num_states);
+    if (!live) return -2;
+    int rc = live_states(num_states, sym_row_ptr, sym_targets, accept, live);
+    if (rc != 0) {
+        free(live);
+        return rc;
+    }
+    walk_job_t job;
+    memset(&job, 0, sizeof(job));
+    job.n = num_states;
+    job.start = start_state;
+    job.srp = sym_row_ptr;
+    job.stg = sym_targets;
+    job.ssy = sym_symbols;
+    job.live = live;
+    job.offsets = offsets;
+    job.n_inputs = n_inputs;
+    job.seed = seed;
+    job.out = out;
+    for (int32_t s = 0; s < num_states; ++s) {
+        const int32_t d = sym_row_ptr[s + 1] - sym_row_ptr[s];
+        if (d > job.max_degree) job.max_degree = d;
+    }
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > 256) n_threads = 256;
+    job.stride = n_threads;
+    pthread_mutex_init(&job.mu, NULL);
+    pthread_t tids[256];
+    int32_t started = 0;
+    for (int32_t t = 1; t < n_threads; ++t) {
+        if (pthread_create(&tids[started], NULL, walk_worker, &job) != 0) break;
+        ++started;
+    }
+    walk_worker(&job); /* also takes the stripes of threads that could not be started */
+    for (int32_t t = 0; t < started; ++t) pthread_join(tids[t], NULL);
+    pthread_mutex_destroy(&job.mu);
+    free(live);
+    return job.failed ? -2 : 0;
+}
+
 int fsm_oracle_version(void) { return 1; }

@@ -123,6 +123,9 @@ def _load():
         lib.fsm_oracle_dfa_batch.restype = ctypes.c_int
         lib.fsm_oracle_dfa_batch.argtypes = [ctypes.c_int32, ctypes.c_int32, p, p, p, p,
                                              ctypes.c_int64, ctypes.c_int32, p, p, p]
+        lib.fsm_oracle_walk.restype = ctypes.c_int
+        lib.fsm_oracle_walk.argtypes = [ctypes.c_int32, p, p, p, p, ctypes.c_int32, p,
+                                        ctypes.c_int64, ctypes.c_uint64, p, ctypes.c_int32]
         _lib = lib
     return _lib
 
@@ -190,6 +193,24 @@ def dfa_batch(dfa, data: np.ndarray, offsets: np.ndarray, threads: int | None = 
     if rc != 0:
         raise ValueError(f"oracle rejected the automaton or offsets (rc={rc})")
     return flags, lens, examined
+
+
+def walk_bytes(nfa, offsets: np.ndarray, seed: int, threads: int | None = None) -> np.ndarray:
+    """Random-walk inputs for ``nfa``, byte-identical to the product library's generator;
+    the CPU reference arm of the benchmark uses this one so that it loads no product code."""
+    lib = _load()
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    total = int(offsets[-1])
+    out = np.zeros(max(total, 1), dtype=np.uint8)
+    arrs = [np.ascontiguousarray(getattr(nfa, f), dtype=np.int32) for f in
+            ("sym_row_ptr", "sym_targets", "sym_symbols")]
+    acc = np.ascontiguousarray(nfa.accept, dtype=np.uint8)
+    rc = lib.fsm_oracle_walk(int(nfa.num_states), *[_ptr(a) for a in arrs], _ptr(acc),
+                             int(nfa.start_state), _ptr(offsets), len(offsets) - 1,
+                             int(seed) & (2**64 - 1), _ptr(out), _threads(threads))
+    if rc != 0:
+        raise ValueError(f"oracle walk rejected its arguments (rc={rc})")
+    return out[:total]
 
 
 def verdicts(automaton, inputs, threads: int | None = None) -> list[tuple[bool, int]]:

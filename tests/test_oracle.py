@@ -133,3 +133,48 @@ def test_generators_are_pinned_and_oracle_matches_reference(name):
         got = O.verdicts(a, b.inputs(sel))
         want = [(bool(v[1]), v[2]) for v in vec["verdicts"] if b.aut_ids[v[0]] == k]
         assert got == want
+
+
+def test_oracle_walker_matches_the_library_walker():
+    """The CPU reference arm generates its random-walk inputs with the oracle's walker
+    (so that it loads no product code); the bytes must equal the library's."""
+    cases = [(W.random_nfa(1024, seed=0, degree=2, accept_prob=0.01), 10),
+             (W.random_nfa(3000, seed=5, poisson=4.0, accept_prob=0.001), 20),
+             (W.c4_automaton(101), 1001)]
+    b = NFABuilder()  # ANY edges and a start state outside the live core
+    s = [b.add_state() for _ in range(5)]
+    b.add_transition(s[0], ANY_SYMBOL, s[1])
+    b.add_transition(s[1], "a", s[2])
+    b.add_transition(s[2], ANY_SYMBOL, s[1])
+    b.add_transition(s[1], "b", s[3])
+    b.set_accept(s[3])
+    cases.append((b.build(), 7))
+    lengths = np.array([0, 1, 17, 300, 5000, 4096, 33, 1], dtype=np.int64)
+    off = W.offsets_of(lengths)
+    for nfa, seed in cases:
+        for threads in (1, 3):
+            ours = O.walk_bytes(nfa, off, seed=seed, threads=threads)
+            lib = W.walk_bytes(nfa, off, seed=seed, threads=2)
+            assert np.array_equal(ours, lib), (nfa.num_states, seed, threads)
+
+
+def test_reference_arm_workload_loads_no_product_library():
+    """bench.py --impl reference builds its workload and times the oracle without
+    mapping libgbfsm.so."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    repo = Path(__file__).resolve().parent.parent
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "b = bench.load_workload('c1-live', reference_arm=True)\n"
+        "from oracle import oracle as O\n"
+        "O.nfa_batch(b.automata[0], b.data, b.offsets)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('libgbfsm' in maps, 'libfsm_oracle' in maps)\n" % str(repo))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=600, cwd=str(repo))
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.split() == ["False", "True"]

@@ -72,6 +72,7 @@ def test_availability_probe_is_replaced_and_explains_itself():
         assert "CUDA device" in out and "raised True" in out
 
 
+@pytest.mark.gpu
 def test_reference_objects_run_through_the_engine_when_a_gpu_is_present():
     out = _run("""
         import torch

@@ -20,11 +20,14 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _run(fn, nfa, d_data, d_off, n, plan, workspace=None):
+def _run(fn, nfa, d_data, d_off, n, plan, workspace=None, out=None):
     import torch
 
     dev = d_data.device
-    out = torch.full((3, n), -7, dtype=torch.int32, device=dev)
+    if out is None:
+        out = torch.full((3, n), -7, dtype=torch.int32, device=dev)
+    else:
+        out.fill_(-7)
     stream = torch.cuda.current_stream(dev).cuda_stream
     args = [ctypes.byref(nfa.desc), d_data.data_ptr(), d_off.data_ptr(), n, ctypes.byref(plan),
             out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr()]
@@ -55,7 +58,13 @@ def _case(automaton, data, offsets, technique, block_threads=0):
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
     want = _run(lib.gbfsm_nfa_run, nfa, d_data, d_off, n, plan, ws)
     first = _run(lib.gbfsm_nfa_run_static, nfa, d_data, d_off, n, plan)
-    second = _run(lib.gbfsm_nfa_run_static, nfa, d_data, d_off, n, plan)
+    # the second call, set-up done, takes no device memory: free memory is unchanged
+    out = torch.empty((3, n), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize(dev)
+    free_before = torch.cuda.mem_get_info(dev)[0]
+    second = _run(lib.gbfsm_nfa_run_static, nfa, d_data, d_off, n, plan, out=out)
+    free_after = torch.cuda.mem_get_info(dev)[0]
+    assert free_after == free_before
     assert np.array_equal(first, want)
     assert np.array_equal(second, want)
     of, ol, oe, _ = O.nfa_batch(automaton, data, offsets)
