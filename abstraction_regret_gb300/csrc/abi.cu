@@ -250,8 +250,55 @@ gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
     if (!table || !tasks || !data || !offsets || !chunk_io || !chunk_io->chunks ||
         !chunk_io->records || !chunk_io->overflow_tasks || !chunk_io->overflow_count)
         return fail(GBFSM_INVALID_ARG, "NULL array passed to gbfsm_lanes_run");
-    return launch_lanes(table, tasks, n_tasks, data, offsets, *chunk_io,
+    return launch_lanes(table, n_automata, tasks, n_tasks, nullptr, data, offsets, *chunk_io,
                         static_cast<cudaStream_t>(stream));
+}
+
+gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_automata,
+                                   const gbfsm_task *tasks, int32_t max_tasks,
+                                   const int32_t *range, const uint8_t *data,
+                                   const int64_t *offsets, const gbfsm_chunk_io *chunk_io,
+                                   void *stream) {
+    if (max_tasks < 0 || n_automata < 0) return fail(GBFSM_INVALID_ARG, "negative task count");
+    if (max_tasks == 0) return GBFSM_OK;
+    if (!table || !tasks || !range || !data || !offsets || !chunk_io || !chunk_io->chunks ||
+        !chunk_io->records || !chunk_io->overflow_tasks || !chunk_io->overflow_count)
+        return fail(GBFSM_INVALID_ARG, "NULL array passed to gbfsm_lanes_run_range");
+    return launch_lanes(table, n_automata, tasks, max_tasks, range, data, offsets, *chunk_io,
+                        static_cast<cudaStream_t>(stream));
+}
+
+size_t gbfsm_batch_plan_scratch_bytes(int32_t n_inputs) {
+    return batch_plan_scratch_bytes(n_inputs);
+}
+
+gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *a, void *stream) {
+    if (!a) return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: NULL arguments");
+    if (a->n_inputs < 0 || a->n_automata < 1)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: %d inputs, %d automata", a->n_inputs,
+                    a->n_automata);
+    if (a->n_inputs == 0) return GBFSM_OK;
+    if (!a->offsets || !a->aut_class || !a->chunks || !a->tasks_lanes || !a->tasks_persist ||
+        !a->tasks_fixup || !a->input_ids || !a->header || !a->scratch)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: NULL array");
+    if (a->min_chunk < 64)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: min_chunk %d below 64", a->min_chunk);
+    if (a->cap_chunks < 1 || a->cap_lane_tasks < 0 || a->cap_persist_tasks < 0 ||
+        a->cap_fixup_tasks < 0)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: negative capacity");
+    if (a->n_slices > GBFSM_PLAN_MAX_SLICES)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: more than %d slices",
+                    GBFSM_PLAN_MAX_SLICES);
+    if (a->n_slices > 1) {
+        if (a->slice_first[0] != 0 || a->slice_first[a->n_slices] != a->n_inputs)
+            return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: slices must cover the inputs");
+        for (int k = 0; k < a->n_slices; ++k)
+            if (a->slice_first[k + 1] < a->slice_first[k])
+                return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: slices out of order");
+        if (!(a->shrink >= 0.0f && a->shrink < 1.0f))
+            return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: shrink must be in [0, 1)");
+    }
+    return launch_batch_plan(*a, static_cast<cudaStream_t>(stream));
 }
 
 size_t gbfsm_persistent_workspace_bytes(int32_t max_words, const gbfsm_plan *plan) {
@@ -276,7 +323,8 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
         return fail(GBFSM_INVALID_ARG, "NULL array passed to gbfsm_persistent_run");
     if (max_words < 1) return fail(GBFSM_INVALID_ARG, "max_words must be >= 1");
     const gbfsm_plan p = plan_or_default(plan, GBFSM_TECH_COMPACT);
-    return launch_persistent(table, max_words, tasks, n_tasks, input_ids, data, offsets, ends,
+    return launch_persistent(table, n_automata, max_words, tasks, n_tasks, input_ids, data,
+                             offsets, ends,
                              chunk_io, flags, lens, examined, workspace,
                              workspace_bytes, p,
                              static_cast<cudaStream_t>(stream));

@@ -66,6 +66,7 @@ struct ChunkIO {
     int32_t *overflow_count;
     const int32_t *task_count;
     int32_t n_chunks;
+    const int32_t *aut_ids;  // per-input automaton (NULL: all 0)
 };
 
 __device__ __forceinline__ uint32_t byte_at(const uint8_t *p) { return __ldg(p); }

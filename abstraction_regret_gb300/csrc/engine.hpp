@@ -65,16 +65,20 @@ gbfsm_status launch_nfa_bitmap(const gbfsm_nfa_dev &a, const BitmapPlan &bp, con
 gbfsm_status launch_dfa_walk(const gbfsm_dfa_dev &d, const gbfsm_plan &p, const uint8_t *data,
                              const int64_t *offsets, int32_t n_inputs, int32_t *flags,
                              int32_t *lens, int32_t *examined, cudaStream_t stream);
-gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
+gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t n_automata,
+                               int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
                                const uint8_t *data, const int64_t *offsets, const int64_t *ends,
                                const gbfsm_chunk_io *chunk_io, int32_t *flags,
                                int32_t *lens, int32_t *examined, void *workspace,
                                size_t workspace_bytes, const gbfsm_plan &p, cudaStream_t stream);
 int lanes_warps_per_sm();
-gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
+gbfsm_status launch_lanes(const gbfsm_automaton *table, int32_t n_automata,
+                          const gbfsm_task *tasks, int32_t n_tasks, const int32_t *range,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream);
+size_t batch_plan_scratch_bytes(int32_t n_inputs);
+gbfsm_status launch_batch_plan(const gbfsm_batch_plan_args &args, cudaStream_t stream);
 size_t persistent_workspace_bytes(int32_t max_words, const gbfsm_plan &p);
 int32_t persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan &p);
 gbfsm_status launch_nfa_layout(int32_t n, const int32_t *srp, const int32_t *stg,

@@ -22,60 +22,86 @@ constexpr int kLanesThreads = 128;
 constexpr int kLanesMinBlocks = GBFSM_LANES_MIN_BLOCKS;  // 8 x 128 threads: 64 registers
 
 __global__ void __launch_bounds__(kLanesThreads, kLanesMinBlocks) lanes_kernel(
-    const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
-    int32_t n_tasks, const uint8_t *__restrict__ data, const int64_t *__restrict__ offsets,
-    ChunkIO io) {
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (warp >= n_tasks) return;
-    const gbfsm_task task = tasks[warp];
-    const int lane = (int)lane_id();
-    if (lane >= task.count) return;
-    const int cid = task.first + lane;
-    if (cid < 0 || cid >= io.n_chunks) return;  // a task naming chunks outside the table
-    const gbfsm_chunk ch = io.chunks[cid];
-    const int64_t off = offsets[ch.input];
-    const gbfsm_automaton &T = table[task.automaton];
-    const gbfsm_nfa_dev &A = T.nfa;
-    if (T.kind != 0) return;  // LANES tasks of a DFA are ignored
-    const bool lane_tables = A.lane_edges != nullptr && A.pair_row != nullptr;
-    bool done = false;
-    if (lane_tables) {
-        const Bounds bd = chunk_bounds(io, A, data + off, cid, off);
-        done = lane_chunk(A, data + off, bd.b, bd.e, bd.ov_end, ch.index, io.records + cid);
+    const gbfsm_automaton *__restrict__ table, int32_t n_automata,
+    const gbfsm_task *__restrict__ tasks, int32_t n_tasks, const int32_t *__restrict__ range,
+    const uint8_t *__restrict__ data, const int64_t *__restrict__ offsets, ChunkIO io) {
+    int32_t first = 0;
+    if (range) {  // a task range written on the device by an earlier launch
+        first = range[0];
+        n_tasks = min(n_tasks, range[1]);
     }
-    if (!done) {
-        gbfsm_task spill;
-        spill.automaton = task.automaton;
-        spill.first = cid;
-        spill.count = 1;
-        spill.kind = GBFSM_TASK_CHUNK;
-        // the queue holds n_chunks entries: only a task list naming a chunk twice could
-        // overflow it, and then the extra entries are dropped rather than written past it
-        const int slot = atomicAdd(io.overflow_count, 1);
-        if (slot < io.n_chunks) io.overflow_tasks[slot] = spill;
+    const int lane = (int)lane_id();
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n_tasks; w += nwarps) {
+        const gbfsm_task task = tasks[first + w];
+        if (lane >= task.count) continue;
+        const int cid = task.first + lane;
+        if (cid < 0 || cid >= io.n_chunks) continue;  // a task naming chunks outside the table
+        const gbfsm_chunk ch = io.chunks[cid];
+        if (ch.input < 0) continue;
+        // automaton -1: each lane runs its chunk's input's automaton
+        const int32_t aut =
+            task.automaton >= 0 ? task.automaton : (io.aut_ids ? io.aut_ids[ch.input] : 0);
+        if (aut < 0 || aut >= n_automata) continue;
+        const int64_t off = offsets[ch.input];
+        const gbfsm_automaton &T = table[aut];
+        const gbfsm_nfa_dev &A = T.nfa;
+        if (T.kind != 0) continue;  // LANES tasks of a DFA are ignored
+        const bool lane_tables = A.lane_edges != nullptr && A.pair_row != nullptr;
+        bool done = false;
+        if (lane_tables) {
+            const Bounds bd = chunk_bounds(io, A, data + off, cid, off);
+            done = lane_chunk(A, data + off, bd.b, bd.e, bd.ov_end, ch.index, io.records + cid);
+        }
+        if (!done) {
+            gbfsm_task spill;
+            spill.automaton = aut;
+            spill.first = cid;
+            spill.count = 1;
+            spill.kind = GBFSM_TASK_CHUNK;
+            // the queue holds n_chunks entries: only a task list naming a chunk twice
+            // could overflow it, and then the extra entries are dropped rather than written
+            // past it
+            const int slot = atomicAdd(io.overflow_count, 1);
+            if (slot < io.n_chunks) io.overflow_tasks[slot] = spill;
+        }
     }
 }
 
 }  // namespace
 
 int lanes_warps_per_sm() {
+    // asked once per device (the answer depends only on the kernel and the device)
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = -1;
+    if (dev >= 0 && cached[dev] > 0) return cached[dev];
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, lanes_kernel, kLanesThreads, 0) !=
         cudaSuccess)
         blocks = 0;
     cudaGetLastError();
-    return blocks * (kLanesThreads / 32);
+    const int warps = blocks * (kLanesThreads / 32);
+    if (dev >= 0 && warps > 0) cached[dev] = warps;
+    return warps;
 }
 
-gbfsm_status launch_lanes(const gbfsm_automaton *table, const gbfsm_task *tasks, int32_t n_tasks,
+gbfsm_status launch_lanes(const gbfsm_automaton *table, int32_t n_automata,
+                          const gbfsm_task *tasks, int32_t n_tasks, const int32_t *range,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream) {
     if (n_tasks <= 0) return GBFSM_OK;
     ChunkIO io{chunk_io.chunks, static_cast<ChunkRecord *>(chunk_io.records),
-               chunk_io.overflow_tasks, chunk_io.overflow_count, nullptr, chunk_io.n_chunks};
+               chunk_io.overflow_tasks, chunk_io.overflow_count, nullptr, chunk_io.n_chunks,
+               chunk_io.aut_ids};
     const int warps_per_block = kLanesThreads / 32;
-    const int grid = (n_tasks + warps_per_block - 1) / warps_per_block;
-    lanes_kernel<<<grid, kLanesThreads, 0, stream>>>(table, tasks, n_tasks, data, offsets, io);
+    int grid = (n_tasks + warps_per_block - 1) / warps_per_block;
+    if (range) {  // at most one resident wave; the warps loop over the tasks
+        const int wave = sm_count() * (lanes_warps_per_sm() / warps_per_block);
+        if (wave > 0 && grid > wave) grid = wave;
+    }
+    lanes_kernel<<<grid, kLanesThreads, 0, stream>>>(table, n_automata, tasks, n_tasks, range,
+                                                      data, offsets, io);
     GBFSM_LAUNCH_CHECK("lanes_kernel launch");
     return GBFSM_OK;
 }

@@ -61,7 +61,8 @@ PersistLayout persist_layout(int32_t max_words, const gbfsm_plan &p) {
 }
 
 __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persistent_kernel(
-    const gbfsm_automaton *__restrict__ table, const gbfsm_task *__restrict__ tasks,
+    const gbfsm_automaton *__restrict__ table, int32_t n_automata,
+    const gbfsm_task *__restrict__ tasks,
     int32_t n_tasks, const int32_t *__restrict__ input_ids, const uint8_t *__restrict__ data,
     const int64_t *__restrict__ offsets, const int64_t *__restrict__ ends, ChunkIO io,
     int32_t *flags, int32_t *lens, int32_t *examined, PersistLayout L, uint32_t *ticket,
@@ -94,6 +95,33 @@ __global__ void __launch_bounds__(kMaxBlockThreads, kPersistMinBlocks) persisten
         t = __shfl_sync(GBFSM_FULL_MASK, t, 0);
         if (t >= (uint32_t)n_tasks) break;
         const gbfsm_task task = tasks[t];
+        if (task.kind == GBFSM_TASK_DFA_GROUP) {  // one walk per lane, each on its own DFA
+            if ((int)lane < task.count) {
+                const int32_t id = input_ids[task.first + (int)lane];
+                const int32_t aut = io.aut_ids ? io.aut_ids[id] : 0;
+                if (aut >= 0 && aut < n_automata && table[aut].kind == 1) {
+                    const gbfsm_dfa_dev d = table[aut].dfa;
+                    const int64_t b = offsets[id];
+                    const int64_t e = ends ? ends[id] : offsets[id + 1];
+                    int32_t f, l;
+                    int64_t ex;
+                    if (d.entry_bytes == 2)
+                        dfa_walk<uint16_t, false>(static_cast<const uint16_t *>(d.table),
+                                                  d.accept_bits, (uint32_t)d.start_state,
+                                                  data + b, e - b, f, l, ex);
+                    else
+                        dfa_walk<uint32_t, false>(static_cast<const uint32_t *>(d.table),
+                                                  d.accept_bits, (uint32_t)d.start_state,
+                                                  data + b, e - b, f, l, ex);
+                    flags[id] = f;
+                    lens[id] = l;
+                    if (examined) examined[id] = (int32_t)ex;
+                }
+            }
+            __syncwarp();
+            continue;
+        }
+        if (task.automaton < 0 || task.automaton >= n_automata) continue;
         const gbfsm_automaton *A = table + task.automaton;
         if (A->kind == 0) {
             const gbfsm_nfa_dev nfa = A->nfa;
@@ -221,7 +249,8 @@ int32_t persistent_ctas_query(const PersistLayout &L, const gbfsm_plan &p) {
 }
 }  // namespace
 
-gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
+gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t n_automata,
+                               int32_t max_words,
                                const gbfsm_task *tasks, int32_t n_tasks, const int32_t *input_ids,
                                const uint8_t *data, const int64_t *offsets, const int64_t *ends,
                                const gbfsm_chunk_io *chunk_io, int32_t *flags,
@@ -240,7 +269,7 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
         return fail(GBFSM_INVALID_ARG, "persistent workspace too small: %zu < %zu bytes",
                     workspace_bytes, need);
     if (n_tasks <= 0) return GBFSM_OK;
-    ChunkIO io{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    ChunkIO io{nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr};
     if (chunk_io) {
         io.chunks = chunk_io->chunks;
         io.records = static_cast<ChunkRecord *>(chunk_io->records);
@@ -248,6 +277,7 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
         io.overflow_count = chunk_io->overflow_count;
         io.task_count = chunk_io->task_count;
         io.n_chunks = chunk_io->n_chunks;
+        io.aut_ids = chunk_io->aut_ids;
     }
     uint32_t *ticket = static_cast<uint32_t *>(workspace);
     uint8_t *gws = static_cast<uint8_t *>(workspace) + 256;
@@ -256,7 +286,8 @@ gbfsm_status launch_persistent(const gbfsm_automaton *table, int32_t max_words,
     int grid = sm_count() * ctas;
     const int needed = (n_tasks + L.wpc - 1) / L.wpc;
     if (grid > needed) grid = needed;
-    persistent_kernel<<<grid, L.wpc * 32, smem, stream>>>(table, tasks, n_tasks, input_ids, data,
+    persistent_kernel<<<grid, L.wpc * 32, smem, stream>>>(table, n_automata, tasks, n_tasks,
+                                                          input_ids, data,
                                                           offsets, ends, io, flags, lens,
                                                           examined, L, ticket, gws);
     GBFSM_LAUNCH_CHECK("persistent_kernel launch");

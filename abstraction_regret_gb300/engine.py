@@ -148,6 +148,203 @@ class DeviceTasks:
         self.n_lane_chunks = int(plan.lane_chunks)
 
 
+class DevicePlan:
+    """Buffers of a batch planned on the device (gbfsm_batch_plan) and its launches.
+
+    Sized for up to ``n_inputs`` inputs of ``total_bytes`` in all. ``plan`` enqueues the
+    two planning launches; ``launch`` then enqueues the lane launch, the persistent
+    launch, the overflow pass and the fix-up, each reading its task count from the plan
+    header on the device -- no host work depends on the batch's lengths, so the whole
+    step (planning included) can be captured once and replayed for new inputs of the
+    same sizes. ``slices`` (input indices where slices start, plus ``n_inputs``) gives
+    each slice's lane tasks their own range in the header, for pipelined ingest.
+    """
+
+    def __init__(self, engine: PersistentEngine, n_inputs: int, total_bytes: int,
+                 slices=None, shrink: float = 0.0) -> None:
+        self.engine = engine
+        dev = engine.device
+        self.n = int(n_inputs)
+        self.total_bytes = int(total_bytes)
+        self.slices = list(slices) if slices is not None and len(slices) > 2 else None
+        if self.slices is not None and len(self.slices) - 1 > native.PLAN_MAX_SLICES:
+            raise ValueError(f"at most {native.PLAN_MAX_SLICES} slices")
+        self.shrink = float(shrink) if self.slices else 0.0
+        lw = engine.sm_count * engine.lane_warps_per_sm
+        pw = engine.resident_warps
+        fixed = engine.fixed_chunk
+        n = max(self.n, 1)
+        if fixed > 0:
+            cap = int(total_bytes) // max(1, fixed // 2) + 2 * n + 64
+        else:
+            # lane chunks fill at most one wave (32 per resident warp) unless even 1 MiB
+            # chunks do not; slices scale lane chunks down by up to 1 - shrink; warp
+            # chunks number fewer than 8 per resident persistent warp plus one per input
+            factor = 1.25 / (1.0 - self.shrink)
+            cap = int(factor * (LANE_GROUP * lw + int(total_bytes) // (1 << 20) + n)) + \
+                8 * pw + 2 * n + 64
+        self.cap_chunks = cap
+        self.cap_lanes = cap // LANE_GROUP + 2
+        self.cap_persist = n + cap
+        self.cap_fixup = n
+        i32 = torch.int32
+        self.chunks = torch.empty(cap * 24, dtype=torch.uint8, device=dev)
+        self.records = torch.empty(cap * native.CHUNK_RECORD_BYTES, dtype=torch.uint8, device=dev)
+        self.overflow = torch.empty(cap * 4, dtype=i32, device=dev)
+        self.tasks = torch.empty((self.cap_lanes + self.cap_persist + self.cap_fixup) * 4,
+                                 dtype=i32, device=dev)
+        self.input_ids = torch.empty(n, dtype=i32, device=dev)
+        self.header = torch.zeros(native.PLAN_HEADER_WORDS, dtype=i32, device=dev)
+        self.h_header = torch.zeros(native.PLAN_HEADER_WORDS, dtype=i32, pin_memory=True)
+        lib = native.lib()
+        self.scratch = torch.empty(max(16, int(lib.gbfsm_batch_plan_scratch_bytes(n))),
+                                   dtype=torch.uint8, device=dev)
+        base = self.tasks.data_ptr()
+        self.tasks_lanes = base
+        self.tasks_persist = base + self.cap_lanes * 16
+        self.tasks_fixup = base + (self.cap_lanes + self.cap_persist) * 16
+
+    @staticmethod
+    def device_bytes(engine: PersistentEngine, n_inputs: int, total_bytes: int) -> int:
+        """Device memory a plan of this size takes (chunk table, records, task queues)."""
+        lw = engine.sm_count * engine.lane_warps_per_sm
+        n = max(int(n_inputs), 1)
+        cap = int(1.25 * (LANE_GROUP * lw + int(total_bytes) // (1 << 20) + n)) + \
+            8 * engine.resident_warps + 2 * n + 64
+        return cap * (24 + native.CHUNK_RECORD_BYTES + 16 + 16) + n * 64
+
+    def _hdr(self, word: int) -> int:
+        return self.header.data_ptr() + 4 * word
+
+    def plan(self, d_off, d_ends, d_aut, stream, n_inputs: int | None = None) -> None:
+        """Enqueue planning for the inputs at ``d_off`` (``d_ends``, ``d_aut``: device
+        tensors or None)."""
+        eng = self.engine
+        n = self.n if n_inputs is None else int(n_inputs)
+        if n > self.n:
+            raise ValueError(f"{n} inputs above the plan's capacity of {self.n}")
+        a = native.BatchPlanArgs()
+        a.n_inputs = n
+        a.n_automata = len(eng.automata)
+        a.offsets = d_off.data_ptr()
+        a.ends = d_ends.data_ptr() if d_ends is not None else None
+        a.aut_ids = d_aut.data_ptr() if d_aut is not None else None
+        a.aut_class = eng.aut_class.data_ptr()
+        a.lane_warps = eng.sm_count * eng.lane_warps_per_sm
+        a.persist_warps = eng.resident_warps
+        a.min_chunk = MIN_CHUNK
+        a.fixed_chunk = eng.fixed_chunk
+        if self.slices:
+            a.n_slices = len(self.slices) - 1
+            a.shrink = self.shrink
+            for k, v in enumerate(self.slices):
+                a.slice_first[k] = int(v)
+        a.cap_chunks = self.cap_chunks
+        a.cap_lane_tasks = self.cap_lanes
+        a.cap_persist_tasks = self.cap_persist
+        a.cap_fixup_tasks = self.cap_fixup
+        a.chunks = self.chunks.data_ptr()
+        a.tasks_lanes = self.tasks_lanes
+        a.tasks_persist = self.tasks_persist
+        a.tasks_fixup = self.tasks_fixup
+        a.input_ids = self.input_ids.data_ptr()
+        a.header = self.header.data_ptr()
+        a.scratch = self.scratch.data_ptr()
+        self._d_aut = d_aut
+        native.check(native.lib().gbfsm_batch_plan(ctypes.byref(a), stream.cuda_stream),
+                     "gbfsm_batch_plan")
+
+    def chunk_io(self, task_count_word: int | None) -> native.ChunkIO:
+        io = native.ChunkIO()
+        io.chunks = self.chunks.data_ptr()
+        io.records = self.records.data_ptr()
+        io.overflow_tasks = self.overflow.data_ptr()
+        io.overflow_count = self._hdr(native.PLAN_OVERFLOW)
+        io.n_chunks = self.cap_chunks
+        io.aut_ids = self._d_aut.data_ptr() if self._d_aut is not None else None
+        if task_count_word is not None:
+            io.task_count = self._hdr(task_count_word)
+        return io
+
+    def launch(self, data_ptr: int, d_off, d_ends, d_flags, d_lens, d_examined, stream,
+               workspace=None, phases: dict | None = None, lane_slices=None) -> int:
+        """Enqueue the four launches of a planned batch; returns their number.
+        ``lane_slices``: ``[(side stream, ready event)]`` per slice (pipelined ingest);
+        slice k's lane tasks run on its side stream once its event has fired."""
+        eng = self.engine
+        lib = native.lib()
+
+        def mark(name):
+            if phases is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record(stream)
+                phases.setdefault(name, []).append(e)
+
+        ws = eng.workspace if workspace is None else workspace
+        table, n_aut = eng.table.data_ptr(), len(eng.automata)
+        io = self.chunk_io(None)
+        launches = 0
+        if lane_slices:
+            fork = torch.cuda.Event()
+            fork.record(stream)
+            joins = []
+            for k, (side, ready) in enumerate(lane_slices):
+                side.wait_event(fork)
+                side.wait_event(ready)
+                st = lib.gbfsm_lanes_run_range(table, n_aut, self.tasks_lanes, self.cap_lanes,
+                                               self._hdr(native.PLAN_SLICES + 2 * k), data_ptr,
+                                               d_off.data_ptr(), ctypes.byref(io),
+                                               side.cuda_stream)
+                native.check(st, "gbfsm_lanes_run_range")
+                done = torch.cuda.Event()
+                done.record(side)
+                joins.append(done)
+                launches += 1
+            for done in joins:
+                stream.wait_event(done)
+            for _, ready in lane_slices:
+                stream.wait_event(ready)
+        else:
+            mark("lanes")
+            st = lib.gbfsm_lanes_run_range(table, n_aut, self.tasks_lanes, self.cap_lanes,
+                                           self._hdr(native.PLAN_LANE_FIRST), data_ptr,
+                                           d_off.data_ptr(), ctypes.byref(io), stream.cuda_stream)
+            native.check(st, "gbfsm_lanes_run_range")
+            mark("lanes")
+            launches += 1
+
+        def persist(name, tasks_ptr, max_tasks, count_word):
+            mark(name)
+            cio = self.chunk_io(count_word)
+            st = lib.gbfsm_persistent_run(
+                table, n_aut, eng.max_words, tasks_ptr, int(max_tasks),
+                self.input_ids.data_ptr(), data_ptr, d_off.data_ptr(),
+                d_ends.data_ptr() if d_ends is not None else None, ctypes.byref(cio),
+                d_flags.data_ptr(), d_lens.data_ptr(),
+                d_examined.data_ptr() if d_examined is not None else None,
+                ws.data_ptr(), eng.ws_bytes, ctypes.byref(eng.plan), stream.cuda_stream)
+            native.check(st, "gbfsm_persistent_run")
+            mark(name)
+
+        persist("persistent", self.tasks_persist, self.cap_persist, native.PLAN_PERSIST_TASKS)
+        persist("overflow", self.overflow.data_ptr(), self.cap_chunks, native.PLAN_OVERFLOW)
+        persist("fixup", self.tasks_fixup, self.cap_fixup, native.PLAN_FIXUP_TASKS)
+        return launches + 3
+
+    def fetch_header(self, stream) -> None:
+        """Enqueue the header's copy to pinned host memory (read it after the stream)."""
+        with torch.cuda.stream(stream):
+            self.h_header.copy_(self.header, non_blocking=True)
+
+    def check(self) -> None:
+        """Raise if the last plan (its header fetched and the stream finished) failed."""
+        st = int(self.h_header[native.PLAN_STATUS])
+        if st == 1:
+            raise RuntimeError("device plan: a plan buffer was too small for this batch")
+        if st == 2:
+            raise ValueError("device plan: a request names an automaton outside the pool")
+
+
 class PersistentEngine:
     """A resident automaton pool plus the persistent launch over it."""
 
@@ -215,6 +412,23 @@ class PersistentEngine:
         self._staging = Staging(self.device)
         self._results = Results(self.device)
         self._tasks = DeviceTasks(self.device)
+        # planning classes of the automata (gbfsm_batch_plan) and the chunk-size rule
+        cls = []
+        for i, k in enumerate(self.kinds):
+            if k is Kind.DFA:
+                cls.append(native.PLAN_DFA)
+            elif self.lane_ok[i]:
+                cls.append(native.PLAN_NFA_LANES)
+            elif self.can_chunk[i]:
+                cls.append(native.PLAN_NFA_WARP)
+            else:
+                cls.append(native.PLAN_NFA_WHOLE)
+        self.aut_class = torch.tensor(cls, dtype=torch.int32, device=self.device)
+        self.fixed_chunk = -1 if chunk_bytes is None else max(0, int(chunk_bytes))
+        if self.fixed_chunk > 0:
+            self.fixed_chunk = max(self.fixed_chunk, MIN_CHUNK)
+        self._dplan: DevicePlan | None = None
+        self._h_aut = self._d_aut = None
 
     # ---- task queue ---------------------------------------------------------------------
 
@@ -479,29 +693,64 @@ class PersistentEngine:
             launches += 1
         return launches
 
+    def device_plan(self, n_inputs: int, total_bytes: int) -> DevicePlan:
+        """Plan buffers for a batch of this size (kept and reused while batches fit)."""
+        p = self._dplan
+        if p is None or p.n < n_inputs or p.total_bytes < total_bytes:
+            n = max(int(n_inputs), 2 * (p.n if p else 0), 64)
+            total = max(int(total_bytes), 2 * (p.total_bytes if p else 0), 1 << 20)
+            self._dplan = None  # free the old buffers first
+            p = DevicePlan(self, n, total)
+            self._dplan = p
+        return p
+
+    def upload_aut_ids(self, aut_ids, stream):
+        """Device int32 copy of the batch's automaton ids (None for a one-automaton pool,
+        whose requests all name automaton 0)."""
+        aut = np.asarray(aut_ids, dtype=np.int64)
+        if aut.size and (aut.min() < 0 or aut.max() >= len(self.automata)):
+            raise ValueError("request names an automaton outside the pool")
+        if len(self.automata) == 1:
+            return None
+        n = max(int(aut.size), 1)
+        if self._h_aut is None or self._h_aut.numel() < n:
+            cap = max(n, 2 * (self._h_aut.numel() if self._h_aut is not None else 0), 256)
+            self._h_aut = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+            self._d_aut = torch.empty(cap, dtype=torch.int32, device=self.device)
+        self._h_aut.numpy()[: aut.size] = aut
+        with torch.cuda.stream(stream):
+            self._d_aut[:n].copy_(self._h_aut[:n], non_blocking=True)
+        return self._d_aut
+
     def run_requests(self, aut_ids, inputs, with_examined: bool = False):
-        """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``.
+        """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``; the batch is planned
+        on the device.
 
         Returns ``(flags, lens, examined | None, kernel_ms, transfer_ms)`` as numpy arrays
-        indexed like ``inputs``.
+        indexed like ``inputs``; ``kernel_ms`` covers the planning and simulation launches.
         """
         t0 = time.perf_counter()
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
-        lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
-        d_data, d_off, _, _ = self._staging.put(inputs, stream)
-        plan = self.make_tasks(np.asarray(aut_ids), lengths)
-        self._tasks.upload(plan, stream)
+        d_aut = self.upload_aut_ids(aut_ids, stream)
+        d_data, d_off, _, total = self._staging.put(inputs, stream)
         self._results.ensure(max(n, 1))
         res = self._results
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        self.launch(d_data, d_off, self._tasks, res.d[0], res.d[1],
-                    res.d[2] if with_examined else None, stream)
+        if n:
+            plan = self.device_plan(n, total)
+            plan.plan(d_off, None, d_aut, stream, n)
+            plan.launch(d_data.data_ptr(), d_off, None, res.d[0], res.d[1],
+                        res.d[2] if with_examined else None, stream)
         e1.record(stream)
         res.fetch(n, stream)
+        if n:
+            plan.fetch_header(stream)
         stream.synchronize()
+        if n:
+            plan.check()
         kernel_ms = e0.elapsed_time(e1)
         total_ms = (time.perf_counter() - t0) * 1e3
         h = res.h.numpy()
@@ -534,10 +783,11 @@ def slice_bounds(offsets: np.ndarray, parts: int) -> list[tuple[int, int]]:
 
 
 class GraphRunner:
-    """A fixed batch captured as one CUDA graph: H2D inputs, the launches, D2H verdicts.
+    """A batch captured as one CUDA graph: H2D inputs, planning, the launches, D2H verdicts.
 
-    The batch (flat uint8 data + int64 offsets + automaton ids) is fixed at construction;
-    ``replay`` re-runs it end to end.
+    The batch (flat uint8 data + int64 offsets + automaton ids) is staged at construction;
+    ``replay`` re-runs it end to end, planning included (gbfsm_batch_plan), so the same
+    graph also serves any new batch of the same sizes written into ``h_data`` / ``h_off``.
     """
 
     INGEST = ("copy", "zero_copy", "pipelined")
@@ -547,7 +797,7 @@ class GraphRunner:
                  shrink: float = 0.75) -> None:
         """``ingest`` says how each replay moves the inputs from the pinned host buffer:
 
-        * ``copy``: one copy-engine transfer, then the launches;
+        * ``copy``: one copy-engine transfer, then planning and the launches;
         * ``zero_copy``: no copy, the simulation kernels read the bytes in place over the
           host link (NVLink-C2C on GB300);
         * ``pipelined``: the inputs are copied in ``parts`` slices of contiguous inputs
@@ -558,7 +808,7 @@ class GraphRunner:
           1 - shrink * k / P: a slice that arrives later has less time left, so its lanes
           get shorter chunks.
 
-        ``kernel_only`` always runs the whole-batch plan on the device copy."""
+        ``kernel_only`` plans and runs the batch on the device copy of the inputs."""
         if ingest not in self.INGEST:
             raise ValueError(f"ingest must be one of {self.INGEST}")
         self.engine = engine
@@ -566,43 +816,25 @@ class GraphRunner:
         n = len(offsets) - 1
         self.n = n
         offsets = np.asarray(offsets, dtype=np.int64)
-        lengths = np.diff(offsets)
-        aut_ids = np.asarray(aut_ids)
-        self.task_plan = engine.make_tasks(aut_ids, lengths)
-        self.slices: list[tuple[int, int, int, int]] = []  # (lo, hi, first task, count)
+        aut_ids = np.asarray(aut_ids, dtype=np.int64)
+        total = int(offsets[-1])
+        self.slices: list[tuple[int, int]] = []  # byte range [lo, hi) of each slice's copy
+        slice_first = None
         if ingest == "pipelined" and n:
             spans = slice_bounds(offsets, parts)
-            base = self.task_plan.lane_chunk_bytes
-            sizes = np.zeros(n, np.int64)
-            for k, (a, b) in enumerate(spans):
-                sizes[a:b] = int(base * (1.0 - shrink * k / len(spans))) // 64 * 64
-            plan = engine.make_tasks(aut_ids, lengths, lane_chunk=sizes)
-            # a LANES task waits for the slice holding the last input it reads
-            firsts = np.asarray([a for a, _ in spans], np.int64)
-            ch_input = plan.chunks["input"].astype(np.int64)
-            tl = plan.tasks_l
-            if tl.shape[0]:
-                last_in = np.maximum.reduceat(ch_input[:plan.lane_chunks], tl[:, 1]) \
-                    if plan.lane_chunks else np.zeros(0, np.int64)
-                dep = np.searchsorted(firsts, last_in, side="right") - 1
-                order = np.argsort(dep, kind="stable")
-                plan.tasks_l = np.ascontiguousarray(tl[order])
-                counts = np.bincount(dep, minlength=len(spans))
-            else:
-                counts = np.zeros(len(spans), np.int64)
-            start = np.concatenate([[0], np.cumsum(counts)[:-1]])
-            total_b = max(16, -(-int(offsets[-1]) // 16) * 16)
+            slice_first = [a for a, _ in spans] + [n]
+            total_b = max(16, -(-total // 16) * 16)
             # slice k ends at the 16-byte block holding its last input's end and the next
             # slice starts there, so no block is copied twice (a block shared by two inputs
             # arrives with the earlier slice, which the later slice's copy follows)
             lo = 0
-            for k, (a, b) in enumerate(spans):
+            for a, b in spans:
                 hi = min(total_b, -(-int(offsets[b]) // 16) * 16)
-                self.slices.append((lo, hi, int(start[k]), int(counts[k])))
+                self.slices.append((lo, hi))
                 lo = hi
-            self.pipe_plan = plan
-            self.pipe_tasks = DeviceTasks(dev)
-        total = int(offsets[-1])
+        self.plan = DevicePlan(engine, max(n, 1), total, slices=slice_first, shrink=shrink)
+        # the resident copy for kernel_only (no slices: every lane task in one range)
+        self.kplan = DevicePlan(engine, max(n, 1), total) if self.slices else self.plan
         padded = max(16, -(-total // 16) * 16)
         self.h_data = torch.zeros(padded, dtype=torch.uint8, pin_memory=True)
         self.h_data.numpy()[:total] = np.asarray(data[:total], dtype=np.uint8)
@@ -611,27 +843,35 @@ class GraphRunner:
         self.d_data = torch.empty_like(self.h_data, device=dev)
         self.d_data.copy_(self.h_data)
         self.d_off = torch.empty_like(self.h_off, device=dev)
+        self.d_off.copy_(self.h_off)
+        self.multi = len(engine.automata) > 1
+        if self.multi:
+            if aut_ids.size and (aut_ids.min() < 0 or aut_ids.max() >= len(engine.automata)):
+                raise ValueError("request names an automaton outside the pool")
+            self.h_aut = torch.from_numpy(aut_ids.astype(np.int32)).pin_memory()
+            self.d_aut = self.h_aut.to(dev)
+        else:
+            self.h_aut = self.d_aut = None
         self.ingest = ingest
         self.host_ptr = (native.device_pointer(self.h_data.data_ptr())
                          if ingest == "zero_copy" else None)
         self.d_out = torch.zeros((3, max(n, 1)), dtype=torch.int32, device=dev)
-        self.tasks = DeviceTasks(dev)
         self.with_examined = with_examined
         self.stream = torch.cuda.Stream(dev)
         if self.slices:
             self.copy_stream = torch.cuda.Stream(dev)
             self.slice_streams = [torch.cuda.Stream(dev) for _ in self.slices]
             self.slice_events = [torch.cuda.Event() for _ in self.slices]
-        plans = [self.pipe_plan] if self.slices else [self.task_plan]
-        self.h2d_bytes = padded + self.h_off.numel() * 8 + sum(
-            (p.tasks_l.shape[0] + p.tasks_a.shape[0] + p.tasks_b.shape[0]) * 16
-            + p.input_ids.size * 4 + p.chunks.shape[0] * 24 for p in plans)
-        self.d2h_bytes = self.h_out.numel() * 4
+        self.h2d_bytes = (0 if ingest == "zero_copy" else padded) + self.h_off.numel() * 8 + \
+            (self.h_aut.numel() * 4 if self.multi else 0)
+        self.d2h_bytes = self.h_out.numel() * 4 + native.PLAN_HEADER_WORDS * 4
         self.launches_per_step = 0
-        # warm-up outside capture (kernel attributes, occupancy queries, module load)
+        # warm-up outside capture (kernel attributes, occupancy queries, module load); the
+        # plan must fit its buffers
         with torch.cuda.stream(self.stream):
             self._body()
         self.stream.synchronize()
+        self.plan.check()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph, stream=self.stream):
             self._body()
@@ -644,33 +884,29 @@ class GraphRunner:
     def _body(self) -> None:
         s = torch.cuda.current_stream(self.engine.device)
         self.d_off.copy_(self.h_off, non_blocking=True)
+        if self.multi:
+            self.d_aut.copy_(self.h_aut, non_blocking=True)
+        f, l, ex = self._outputs(0)
         if self.slices:
-            # the small task tables first, so they do not queue behind the input slices
-            self.pipe_tasks.upload(self.pipe_plan, s)
             start = torch.cuda.Event()
             start.record(s)
             self.copy_stream.wait_event(start)
             with torch.cuda.stream(self.copy_stream):
-                for (lo, hi, _, _), ev in zip(self.slices, self.slice_events):
+                for (lo, hi), ev in zip(self.slices, self.slice_events):
                     self.d_data[lo:hi].copy_(self.h_data[lo:hi], non_blocking=True)
                     ev.record(self.copy_stream)
-            if not self.pipe_plan.tasks_l.shape[0]:
-                s.wait_stream(self.copy_stream)  # no lane launch to wait for the slices
-            f, l, ex = self._outputs(0)
-            lane_slices = [(first, count, side, ev) for (_, _, first, count), side, ev
-                           in zip(self.slices, self.slice_streams, self.slice_events)]
-            self.launches_per_step = self.engine.launch(self.d_data, self.d_off,
-                                                        self.pipe_tasks, f, l, ex, s,
-                                                        lane_slices=lane_slices)
+            self.plan.plan(self.d_off, None, self.d_aut, s, self.n)
+            self.launches_per_step = 2 + self.plan.launch(
+                self.d_data.data_ptr(), self.d_off, None, f, l, ex, s,
+                lane_slices=list(zip(self.slice_streams, self.slice_events)))
         else:
             if self.ingest == "copy":
                 self.d_data.copy_(self.h_data, non_blocking=True)
-            self.tasks.upload(self.task_plan, s)
-            f, l, ex = self._outputs(0)
-            self.launches_per_step = self.engine.launch(
-                self.host_ptr if self.ingest == "zero_copy" else self.d_data, self.d_off,
-                self.tasks, f, l, ex, s)
+            self.plan.plan(self.d_off, None, self.d_aut, s, self.n)
+            data_ptr = self.host_ptr if self.ingest == "zero_copy" else self.d_data.data_ptr()
+            self.launches_per_step = 2 + self.plan.launch(data_ptr, self.d_off, None, f, l, ex, s)
         self.h_out.copy_(self.d_out, non_blocking=True)
+        self.plan.fetch_header(s)
 
     def replay(self) -> None:
         """Launch the captured graph on the runner's stream (asynchronous)."""
@@ -678,16 +914,36 @@ class GraphRunner:
             self.graph.replay()
 
     def kernel_only(self, stream=None, phases: dict | None = None) -> int:
-        """The launches alone on resident inputs (for device-side timing)."""
+        """Planning and the launches alone, on the device copy of the inputs (for
+        device-side timing); returns the number of kernels launched."""
         stream = stream or torch.cuda.current_stream(self.engine.device)
-        if not self.tasks.na + self.tasks.nb + self.tasks.nl and self.task_plan.input_ids.size:
-            self.tasks.upload(self.task_plan, stream)
         f, l, ex = self._outputs(0)
-        return self.engine.launch(self.d_data, self.d_off, self.tasks, f, l, ex, stream,
-                                  phases=phases)
+        if phases is not None:
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            phases.setdefault("plan", []).append(e)
+        self.kplan.plan(self.d_off, None, self.d_aut, stream, self.n)
+        if phases is not None:
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            phases["plan"].append(e)
+        return 2 + self.kplan.launch(self.d_data.data_ptr(), self.d_off, None, f, l, ex, stream,
+                                     phases=phases)
+
+    def plan_info(self) -> dict:
+        """Chunk sizes and counts of the last plan (after the stream has finished)."""
+        h = self.plan.h_header.numpy()
+        return {"lane_chunk_bytes": int(h[native.PLAN_LANE_BYTES]),
+                "warp_chunk_bytes": int(h[native.PLAN_WARP_BYTES]),
+                "lane_chunks": int(h[native.PLAN_LANE_CHUNKS]),
+                "chunks": int(h[native.PLAN_CHUNKS]),
+                "lane_tasks": int(h[native.PLAN_LANE_TASKS]),
+                "persistent_tasks": int(h[native.PLAN_PERSIST_TASKS]),
+                "fixup_tasks": int(h[native.PLAN_FIXUP_TASKS])}
 
     def verdicts(self):
         """(flags, lens, examined) of the last replay, once it has finished."""
         self.stream.synchronize()
+        self.plan.check()
         h = self.h_out.numpy()
         return h[0, :self.n].copy(), h[1, :self.n].copy(), h[2, :self.n].copy()

@@ -122,10 +122,40 @@ class Chunk(ctypes.Structure):
 class ChunkIO(ctypes.Structure):
     _fields_ = [("chunks", ctypes.c_void_p), ("records", ctypes.c_void_p),
                 ("overflow_tasks", ctypes.c_void_p), ("overflow_count", ctypes.c_void_p),
-                ("task_count", ctypes.c_void_p), ("n_chunks", ctypes.c_int32)]
+                ("task_count", ctypes.c_void_p), ("n_chunks", ctypes.c_int32),
+                ("aut_ids", ctypes.c_void_p)]
 
 
-TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES = 0, 1, 2, 3
+PLAN_MAX_SLICES = 16  # GBFSM_PLAN_MAX_SLICES
+
+
+class BatchPlanArgs(ctypes.Structure):
+    _fields_ = [
+        ("n_inputs", ctypes.c_int32), ("n_automata", ctypes.c_int32),
+        ("offsets", ctypes.c_void_p), ("ends", ctypes.c_void_p),
+        ("aut_ids", ctypes.c_void_p), ("aut_class", ctypes.c_void_p),
+        ("lane_warps", ctypes.c_int32), ("persist_warps", ctypes.c_int32),
+        ("min_chunk", ctypes.c_int32), ("fixed_chunk", ctypes.c_int32),
+        ("n_slices", ctypes.c_int32), ("shrink", ctypes.c_float),
+        ("slice_first", ctypes.c_int32 * (PLAN_MAX_SLICES + 1)),
+        ("cap_chunks", ctypes.c_int32), ("cap_lane_tasks", ctypes.c_int32),
+        ("cap_persist_tasks", ctypes.c_int32), ("cap_fixup_tasks", ctypes.c_int32),
+        ("chunks", ctypes.c_void_p), ("tasks_lanes", ctypes.c_void_p),
+        ("tasks_persist", ctypes.c_void_p), ("tasks_fixup", ctypes.c_void_p),
+        ("input_ids", ctypes.c_void_p), ("header", ctypes.c_void_p),
+        ("scratch", ctypes.c_void_p),
+    ]
+
+
+# automaton classes and header words of gbfsm_batch_plan
+PLAN_NFA_WHOLE, PLAN_NFA_WARP, PLAN_NFA_LANES, PLAN_DFA = 0, 1, 2, 3
+PLAN_HEADER_WORDS = 64
+(PLAN_STATUS, PLAN_LANE_CHUNKS, PLAN_CHUNKS, PLAN_LANE_FIRST, PLAN_LANE_TASKS,
+ PLAN_PERSIST_TASKS, PLAN_FIXUP_TASKS, PLAN_LANE_BYTES, PLAN_WARP_BYTES, PLAN_OVERFLOW,
+ PLAN_WHOLE, PLAN_DFA_INPUTS) = range(12)
+PLAN_SLICES = 16
+
+TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES, TASK_DFA_GROUP = 0, 1, 2, 3, 4
 LANE_CAPACITY = 4  # members a lane holds (kLaneSlots)
 CHUNK_RECORD_BYTES = 256
 STATIC_SCRATCH_BYTES = 32 << 20  # GBFSM_STATIC_SCRATCH_BYTES
@@ -175,13 +205,17 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_nfa_run_static": (ctypes.c_int, [_P(NfaDev), _vp, _vp, _i32, _P(Plan), _vp, _vp,
                                             _vp, _vp]),
     "gbfsm_workload_walk": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _u64, _vp, _i32]),
+    "gbfsm_lanes_run_range": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _P(ChunkIO),
+                                             _vp]),
+    "gbfsm_batch_plan_scratch_bytes": (_sz, [_i32]),
+    "gbfsm_batch_plan": (ctypes.c_int, [_P(BatchPlanArgs), _vp]),
     "gbfsm_probe_l2_read": (ctypes.c_int, [_vp, _sz, _i32, _vp, _vp]),
     "gbfsm_probe_gather16": (ctypes.c_int, [_vp, _sz, _i64, _i32, _vp, _vp]),
     "gbfsm_probe_chase": (ctypes.c_int, [_vp, ctypes.c_uint32, _i64, _i32, _vp, _vp]),
     "gbfsm_probe_smem": (ctypes.c_int, [_i64, _i32, _vp, _vp]),
 }
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 _lib: ctypes.CDLL | None = None
 

@@ -37,7 +37,7 @@ import numpy as np
 import torch
 
 from . import native
-from .engine import DeviceTasks, PersistentEngine
+from .engine import DevicePlan, PersistentEngine
 from .packing import PAD
 from .registry import Kind
 
@@ -47,6 +47,7 @@ class ServeStats:
     requests: int
     wall_s: float
     offered_bytes: int
+    examined_bytes: int
     p50_ms: float
     p99_ms: float
     mean_ms: float
@@ -61,11 +62,18 @@ class ServeStats:
     def offered_GBps(self) -> float:
         return self.offered_bytes / max(self.wall_s, 1e-9) / 1e9
 
+    @property
+    def examined_GBps(self) -> float:
+        """Bytes the simulations consumed (up to each latch or death) per second."""
+        return self.examined_bytes / max(self.wall_s, 1e-9) / 1e9
+
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k in ("requests", "wall_s", "offered_bytes", "p50_ms",
-                                           "p99_ms", "mean_ms", "max_ms", "batches",
-                                           "mean_batch", "rejected", "mode")}
+        d = {k: getattr(self, k) for k in ("requests", "wall_s", "offered_bytes",
+                                           "examined_bytes", "p50_ms", "p99_ms", "mean_ms",
+                                           "max_ms", "batches", "mean_batch", "rejected",
+                                           "mode")}
         d["offered_GBps"] = self.offered_GBps
+        d["examined_GBps"] = self.examined_GBps
         d.update(self.extra)
         return d
 
@@ -83,9 +91,11 @@ class _Slot:
             self.d_data = torch.empty(batch_bytes + PAD, dtype=torch.uint8, device=dev)
         self.h_off = torch.empty(2 * max_requests + 1, dtype=torch.int64, pin_memory=True)
         self.d_off = torch.empty(2 * max_requests + 1, dtype=torch.int64, device=dev)
-        self.tasks = DeviceTasks(dev)
-        self.h_out = torch.zeros((2, max_requests), dtype=torch.int32, pin_memory=True)
-        self.d_out = torch.zeros((2, max_requests), dtype=torch.int32, device=dev)
+        self.h_aut = torch.empty(max_requests, dtype=torch.int32, pin_memory=True)
+        self.d_aut = torch.empty(max_requests, dtype=torch.int32, device=dev)
+        self.plan = DevicePlan(engine, max_requests, batch_bytes)
+        self.h_out = torch.zeros((3, max_requests), dtype=torch.int32, pin_memory=True)
+        self.d_out = torch.zeros((3, max_requests), dtype=torch.int32, device=dev)
         self.reqs: list[int] = []
 
 
@@ -100,7 +110,8 @@ class Server:
         free, _total = torch.cuda.mem_get_info(dev)
         # admission budget: the slots' input buffers must fit a fraction of free memory
         budget = int(free * memory_fraction)
-        per_slot = batch_bytes + 64 * max_requests + self.engine.ws_bytes
+        plan_bytes = DevicePlan.device_bytes(self.engine, max_requests, batch_bytes)
+        per_slot = batch_bytes + 64 * max_requests + self.engine.ws_bytes + plan_bytes
         if slots * per_slot > budget:
             slots = max(1, budget // per_slot)
         self.batch_bytes = batch_bytes
@@ -115,15 +126,13 @@ class Server:
     def _launch(self, slot: _Slot, reqs: list[int], aut_ids: np.ndarray, starts: np.ndarray,
                 lengths: np.ndarray, pool: np.ndarray, pool_dev_ptr: int | None) -> None:
         n = len(reqs)
-        a = aut_ids[reqs]
         ln = lengths[reqs]
+        slot.h_aut.numpy()[:n] = aut_ids[reqs]
+        off = slot.h_off.numpy()
         if self.zero_copy:
-            plan = self.engine.make_tasks(a, ln, starts[reqs])
-            off = slot.h_off.numpy()
             off[:n] = starts[reqs]
             off[n:2 * n] = starts[reqs] + ln
         else:
-            off = slot.h_off.numpy()
             off[0] = 0
             np.cumsum(ln, out=off[1:n + 1])
             h = slot.h_data.numpy()
@@ -133,7 +142,6 @@ class Server:
                 h[pos:pos + k] = pool[s:s + k]
                 pos += k
             h[pos:pos + PAD] = 0
-            plan = self.engine.make_tasks(a, ln)
         with torch.cuda.stream(slot.stream):
             if self.zero_copy:
                 slot.d_off[:2 * n].copy_(slot.h_off[:2 * n], non_blocking=True)
@@ -144,12 +152,14 @@ class Server:
                 used = int(off[n]) + PAD
                 slot.d_data[:used].copy_(slot.h_data[:used], non_blocking=True)
                 slot.d_off[:n + 1].copy_(slot.h_off[:n + 1], non_blocking=True)
-                d_off, d_ends, data = slot.d_off, None, slot.d_data
-            slot.tasks.upload(plan, slot.stream)
-            self.engine.launch(data, d_off, slot.tasks, slot.d_out[0], slot.d_out[1], None,
-                               slot.stream, d_ends=d_ends, workspace=slot.workspace)
-            for r in range(2):
+                d_off, d_ends, data = slot.d_off, None, slot.d_data.data_ptr()
+            slot.d_aut[:n].copy_(slot.h_aut[:n], non_blocking=True)
+            slot.plan.plan(d_off, d_ends, slot.d_aut, slot.stream, n)
+            slot.plan.launch(data, d_off, d_ends, slot.d_out[0], slot.d_out[1], slot.d_out[2],
+                             slot.stream, workspace=slot.workspace)
+            for r in range(3):
                 slot.h_out[r, :n].copy_(slot.d_out[r, :n], non_blocking=True)
+            slot.plan.fetch_header(slot.stream)
             slot.event.record(slot.stream)
         slot.reqs = reqs
 
@@ -172,6 +182,7 @@ class Server:
             pool_ptr = native.device_pointer(pinned_pool.data_ptr())
         flags = np.zeros(n, np.int32)
         lens = np.zeros(n, np.int32)
+        examined = np.zeros(n, np.int64)
         done_at = np.zeros(n, np.float64)
         rejected = np.zeros(n, dtype=bool)
         pending: deque[int] = deque()
@@ -197,9 +208,11 @@ class Server:
                 if slot.event.query():
                     k = len(slot.reqs)
                     t = time.perf_counter() - t0
+                    slot.plan.check()
                     h = slot.h_out.numpy()
                     flags[slot.reqs] = h[0, :k]
                     lens[slot.reqs] = h[1, :k]
+                    examined[slot.reqs] = h[2, :k]
                     done_at[slot.reqs] = t
                     finished += k
                     busy.remove(slot)
@@ -233,7 +246,7 @@ class Server:
             raise TimeoutError("a bounded device wait gave up during serving")
         stats = ServeStats(
             requests=n, wall_s=wall, offered_bytes=int(lengths[ok].sum()),
-            p50_ms=float(np.percentile(lat[ok], 50)) if ok.any() else 0.0,
+            examined_bytes=int(examined[ok].sum()), p50_ms=float(np.percentile(lat[ok], 50)) if ok.any() else 0.0,
             p99_ms=float(np.percentile(lat[ok], 99)) if ok.any() else 0.0,
             mean_ms=float(lat[ok].mean()) if ok.any() else 0.0,
             max_ms=float(lat[ok].max()) if ok.any() else 0.0,
@@ -252,6 +265,7 @@ def serve_plain(engine: PersistentEngine, trace, executors: dict, time_scale: fl
     arrivals = np.asarray(trace.arrivals, dtype=np.float64) * time_scale
     flags = np.zeros(n, np.int32)
     lens = np.zeros(n, np.int32)
+    examined = np.zeros(n, np.int64)
     done_at = np.zeros(n)
     t0 = time.perf_counter()
     for i in range(n):
@@ -259,13 +273,13 @@ def serve_plain(engine: PersistentEngine, trace, executors: dict, time_scale: fl
         if arrivals[i] > now:
             time.sleep(arrivals[i] - now)
         a, data = trace.request(i)
-        f, l, _, _, _ = executors[a].run_arrays([data])
-        flags[i], lens[i] = f[0], l[0]
+        f, l, e, _, _ = executors[a].run_arrays([data], with_examined=True)
+        flags[i], lens[i], examined[i] = f[0], l[0], e[0]
         done_at[i] = time.perf_counter() - t0
     wall = time.perf_counter() - t0
     lat = (done_at - arrivals) * 1e3
     stats = ServeStats(requests=n, wall_s=wall, offered_bytes=int(np.sum(trace.lengths)),
-                       p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
+                       examined_bytes=int(examined.sum()), p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
                        mean_ms=float(lat.mean()), max_ms=float(lat.max()), batches=n,
                        mean_batch=1.0, rejected=0, mode="plain per request")
     return flags, lens, lat, stats

@@ -461,7 +461,8 @@ def main(argv=None) -> int:
     top = max(phase_ms, key=phase_ms.get) if phase_ms else "lanes"
     kernel_ms = phase_ms.get(top, ms)
     kernel_name = {"lanes": "lanes_kernel", "persistent": "persistent_kernel",
-                   "overflow": "persistent_kernel", "fixup": "persistent_kernel"}[top]
+                   "overflow": "persistent_kernel", "fixup": "persistent_kernel",
+                   "plan": "plan_scan_kernel"}[top]
     # algorithmic bytes of the exact simulation (CSR view): per examined symbol 1 input
     # byte, per active state an 8-byte row range, per scanned edge 8 bytes (symbol +
     # target); 12 bytes of verdicts per input. Counted by the oracle on the same batch.
@@ -480,8 +481,8 @@ def main(argv=None) -> int:
     # input stream alone against HBM; and a latency bound: every lane chain waits for one
     # dependent L2 record load per byte, so at most chains / L2 latency symbols per second
     l2 = onchip.get("l2_read_GBps") if onchip else None
-    chains = min(int(runner.task_plan.lane_chunks),
-                 eng.sm_count * eng.lane_warps_per_sm * 32) if runner.task_plan.lane_chunks else 0
+    info = runner.plan_info()
+    chains = min(info["lane_chunks"], eng.sm_count * eng.lane_warps_per_sm * 32)
     lat_ns = onchip.get("l2_latency_ns") if onchip else None
     symbols = gate.get("examined_bytes", examined_bytes)
     roofline = {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
@@ -512,10 +513,10 @@ def main(argv=None) -> int:
                            "offered_bytes": offered, "examined_bytes": examined_bytes,
                            "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}",
-                           "technique": f"lane chunks of {runner.task_plan.lane_chunk_bytes} B "
-                                        f"({runner.task_plan.lane_chunks} of "
-                                        f"{runner.task_plan.chunks.shape[0]} chunks), "
-                                        "overlap-linked parallel fix-up"},
+                           "technique": f"planned on the device: lane chunks of "
+                                        f"{info['lane_chunk_bytes']} B ({info['lane_chunks']} "
+                                        f"of {info['chunks']} chunks), overlap-linked "
+                                        "parallel fix-up"},
                 "phases_ms": phase_ms,
                 "e2e": e2e, "e2e_other_ingest": e2e_other, "gpu_launches": launches,
                 "oracle_gate": gate,

@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define GBFSM_ABI_VERSION 1
+#define GBFSM_ABI_VERSION 2
 #define GBFSM_ANY_SYMBOL 256 /* src/gpufsm/core/nfa.py:16 */
 #define GBFSM_WORD_BITS 64   /* src/gpufsm/core/packing.py:21 */
 
@@ -281,7 +281,12 @@ typedef struct gbfsm_task {
 #define GBFSM_TASK_WHOLE 0
 #define GBFSM_TASK_CHUNK 1
 #define GBFSM_TASK_FIXUP 2
-#define GBFSM_TASK_LANES 3 /* chunks[first .. first + count), count <= 32, one per lane */
+#define GBFSM_TASK_LANES 3 /* chunks[first .. first + count), count <= 32, one per lane; with
+                              automaton -1 each lane runs its chunk's input's automaton
+                              (gbfsm_chunk_io.aut_ids) */
+#define GBFSM_TASK_DFA_GROUP 4 /* inputs input_ids[first .. first + count), count <= 32, one
+                                  DFA walk per lane, each on its input's own DFA
+                                  (gbfsm_chunk_io.aut_ids); automaton is -1 */
 
 /* A piece of an NFA input: bytes data[begin .. end) of input `input`; `index` counts the
  * input's chunks from 0. Chunks after the first must start at least 2 bytes into the
@@ -306,7 +311,11 @@ typedef struct gbfsm_chunk_io {
                                      the launch that runs LANES tasks */
     const int32_t *task_count;    /* non-NULL: run min(*task_count, n_tasks) tasks, a count
                                      written on the device by an earlier launch */
-    int32_t n_chunks;             /* entries of the chunk table */
+    int32_t n_chunks;             /* entries of the chunk table (its capacity, when a
+                                     device-built table ends with a sentinel chunk whose
+                                     index is 0) */
+    const int32_t *aut_ids;       /* per-input automaton (device, n_inputs), for LANES tasks
+                                     with automaton -1 and DFA_GROUP tasks; NULL = all 0 */
 } gbfsm_chunk_io;
 
 /* Scratch bytes for a persistent launch whose largest NFA has `max_words` set words. */
@@ -352,6 +361,93 @@ gbfsm_status gbfsm_lanes_run(const gbfsm_automaton *table, int32_t n_automata,
                              const gbfsm_task *tasks, int32_t n_tasks, const uint8_t *data,
                              const int64_t *offsets, const gbfsm_chunk_io *chunk_io,
                              void *stream);
+
+/* gbfsm_lanes_run with the task range read on the device: tasks[range[0] .. range[0] +
+ * min(range[1], max_tasks)) run, `range` a device int32[2] written by an earlier launch
+ * (e.g. a slice's range in a gbfsm_batch_plan header). Resident warps loop over the tasks,
+ * so any count runs. No counterpart in the reference. */
+gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_automata,
+                                   const gbfsm_task *tasks, int32_t max_tasks,
+                                   const int32_t *range, const uint8_t *data,
+                                   const int64_t *offsets, const gbfsm_chunk_io *chunk_io,
+                                   void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * Device-side batch planning (no counterpart in the reference, which launches once per
+ * automaton with a thread or warp per whole input). gbfsm_batch_plan builds a batch's
+ * whole task queue on the GPU from its offsets and automaton ids -- chunk sizes, the
+ * chunk table, the LANES, persistent (WHOLE / CHUNK / DFA_GROUP, longest work first by
+ * log2 buckets) and FIXUP tasks, and the input ids -- and writes the counts into a
+ * device header that the launches read (gbfsm_lanes_run_range and the task_count of
+ * gbfsm_chunk_io), so a step needs no host work and a captured graph re-plans on every
+ * replay. Planning costs two small launches (one CTA, then a warp per input).
+ * ------------------------------------------------------------------------------- */
+
+/* Automaton classes for planning (gbfsm_batch_plan_args.aut_class). */
+#define GBFSM_PLAN_NFA_WHOLE 0 /* NFA inputs run whole, a warp each */
+#define GBFSM_PLAN_NFA_WARP 1  /* NFA: inputs of two chunks or more cut into warp chunks
+                                  (the automaton needs first_row / first_edges) */
+#define GBFSM_PLAN_NFA_LANES 2 /* NFA: every input cut into lane chunks (the automaton
+                                  needs the lane tables) */
+#define GBFSM_PLAN_DFA 3       /* DFA inputs, 32 per task, one walk per lane */
+
+/* Words of the plan header (int32, device). */
+#define GBFSM_PLAN_HEADER_WORDS 64
+#define GBFSM_PLAN_STATUS 0        /* 0 ok; 1 a capacity was too small; 2 an automaton id
+                                      out of range. Not 0: every count below is 0. */
+#define GBFSM_PLAN_LANE_CHUNKS 1   /* chunks run one per lane: chunks[0 .. this) */
+#define GBFSM_PLAN_CHUNKS 2        /* all chunks (lane chunks, then warp chunks) */
+#define GBFSM_PLAN_LANE_FIRST 3    /* always 0: {LANE_FIRST, LANE_TASKS} is the range of
+                                      every LANES task for gbfsm_lanes_run_range */
+#define GBFSM_PLAN_LANE_TASKS 4
+#define GBFSM_PLAN_PERSIST_TASKS 5 /* task_count of the persistent launch */
+#define GBFSM_PLAN_FIXUP_TASKS 6   /* task_count of the fix-up launch */
+#define GBFSM_PLAN_LANE_BYTES 7    /* chosen lane chunk size (before slice scaling) */
+#define GBFSM_PLAN_WARP_BYTES 8    /* chosen warp chunk size */
+#define GBFSM_PLAN_OVERFLOW 9      /* zeroed: the overflow_count of the lane launch */
+#define GBFSM_PLAN_WHOLE 10        /* whole NFA inputs: input_ids[0 .. this) */
+#define GBFSM_PLAN_DFA_INPUTS 11   /* DFA inputs: input_ids[WHOLE .. WHOLE + this) */
+#define GBFSM_PLAN_SLICES 16       /* {first, count} LANES task range of slice k at
+                                      16 + 2k, for gbfsm_lanes_run_range */
+#define GBFSM_PLAN_MAX_SLICES 16
+
+typedef struct gbfsm_batch_plan_args {
+    int32_t n_inputs;
+    int32_t n_automata;
+    const int64_t *offsets;   /* device [n_inputs + 1]: input i starts at offsets[i] */
+    const int64_t *ends;      /* device [n_inputs] or NULL: input i ends at ends[i], else at
+                                 offsets[i + 1] */
+    const int32_t *aut_ids;   /* device [n_inputs] or NULL (all automaton 0) */
+    const int32_t *aut_class; /* device [n_automata]: GBFSM_PLAN_* */
+    int32_t lane_warps;       /* resident warps of the lane launch (SMs x
+                                 gbfsm_lanes_warps_per_sm) */
+    int32_t persist_warps;    /* resident warps of the persistent launch */
+    int32_t min_chunk;        /* shortest chunk (bytes) */
+    int32_t fixed_chunk;      /* > 0: every chunk size; 0: chosen; < 0: never chunk */
+    int32_t n_slices;         /* 0 or 1: one lane range; else inputs cut into slices at
+                                 slice_first (host values, ascending, slice_first[0] = 0,
+                                 slice_first[n_slices] = n_inputs) */
+    float shrink;             /* lane chunks of slice k get the size x (1 - shrink k / n) */
+    int32_t slice_first[GBFSM_PLAN_MAX_SLICES + 1];
+    int32_t cap_chunks;       /* capacities of the output arrays */
+    int32_t cap_lane_tasks;
+    int32_t cap_persist_tasks;
+    int32_t cap_fixup_tasks;
+    gbfsm_chunk *chunks;          /* device [cap_chunks] */
+    gbfsm_task *tasks_lanes;      /* device [cap_lane_tasks] */
+    gbfsm_task *tasks_persist;    /* device [cap_persist_tasks] */
+    gbfsm_task *tasks_fixup;      /* device [cap_fixup_tasks] */
+    int32_t *input_ids;           /* device [n_inputs] */
+    int32_t *header;              /* device [GBFSM_PLAN_HEADER_WORDS] */
+    void *scratch;                /* device, gbfsm_batch_plan_scratch_bytes(n_inputs) */
+} gbfsm_batch_plan_args;
+
+/* Scratch bytes gbfsm_batch_plan needs for n_inputs inputs. */
+size_t gbfsm_batch_plan_scratch_bytes(int32_t n_inputs);
+
+/* Enqueue the planning launches on `stream`. Validates the arguments on the host;
+ * device-side failures (capacity, automaton ids) are reported in the header's status. */
+gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *args, void *stream);
 
 /* Occupancy query for persistent launches: CTAs of `plan` resident per SM. */
 int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan);

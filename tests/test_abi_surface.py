@@ -66,13 +66,23 @@ def test_struct_layouts_match_the_header(tmp_path):
              "gbfsm_dfa_dev": native.DfaDev, "gbfsm_plan": native.Plan,
              "gbfsm_automaton": native.Automaton, "gbfsm_task": native.Task,
              "gbfsm_chunk": native.Chunk, "gbfsm_chunk_io": native.ChunkIO,
-             "gbfsm_lane_rec": native.LaneRec}
+             "gbfsm_lane_rec": native.LaneRec, "gbfsm_batch_plan_args": native.BatchPlanArgs}
     src = tmp_path / "probe.c"
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gbfsm.h"', "int main(void) {"]
     for name in pairs:
         lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
     lines.append('  printf("record %d\\n", GBFSM_CHUNK_RECORD_BYTES);')
     lines.append('  printf("static %u\\n", GBFSM_STATIC_SCRATCH_BYTES);')
+    for name in ("STATUS", "LANE_CHUNKS", "CHUNKS", "LANE_FIRST", "LANE_TASKS",
+                 "PERSIST_TASKS", "FIXUP_TASKS", "LANE_BYTES", "WARP_BYTES", "OVERFLOW",
+                 "WHOLE", "DFA_INPUTS", "SLICES", "MAX_SLICES", "HEADER_WORDS", "NFA_WHOLE",
+                 "NFA_WARP", "NFA_LANES", "DFA"):
+        lines.append(f'  printf("PLAN_{name} %d\\n", GBFSM_PLAN_{name});')
+    lines.append('  printf("TASK_DFA_GROUP %d\\n", GBFSM_TASK_DFA_GROUP);')
+    for field in ("slice_first", "cap_chunks", "chunks", "scratch"):
+        lines.append(f'  printf("off_{field} %zu\\n", '
+                     f'offsetof(gbfsm_batch_plan_args, {field}));')
+    lines.append('  printf("off_aut_ids %zu\\n", offsetof(gbfsm_chunk_io, aut_ids));')
     lines.append("  return 0; }")
     src.write_text("\n".join(lines))
     exe = tmp_path / "probe"
@@ -84,6 +94,12 @@ def test_struct_layouts_match_the_header(tmp_path):
     assert int(out["record"]) == native.CHUNK_RECORD_BYTES
     assert int(out["static"]) == native.STATIC_SCRATCH_BYTES
     assert np.dtype(native.CHUNK_DTYPE).itemsize == ctypes.sizeof(native.Chunk)
+    for key, value in out.items():
+        if key.startswith(("PLAN_", "TASK_")):
+            assert int(value) == getattr(native, key), key
+    for field in ("slice_first", "cap_chunks", "chunks", "scratch"):
+        assert int(out[f"off_{field}"]) == getattr(native.BatchPlanArgs, field).offset, field
+    assert int(out["off_aut_ids"]) == native.ChunkIO.aut_ids.offset
 
 
 def test_invalid_arguments_return_status_codes(lib):

@@ -316,7 +316,9 @@ def test_lane_chunks_that_outgrow_the_lane_fall_back_to_warps():
     eng = PersistentEngine([nfa], chunk_bytes=512, lane_pair_mean=float("inf"))
     assert eng.make_tasks(np.zeros(lengths.size), lengths).lane_chunks > 0
     f, l, e, _, _ = eng.run_requests(np.zeros(lengths.size), inputs, with_examined=True)
-    assert int(eng._tasks.d_overflow_count[0].item()) > 0
+    from abstraction_regret_gb300 import native
+
+    assert int(eng._dplan.header[native.PLAN_OVERFLOW].item()) > 0
     of, ol, oe, _ = O.nfa_batch(nfa, data, off)
     assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
 
@@ -371,5 +373,12 @@ def test_graph_runner_ingest_paths(ingest):
         f, l, e = r.verdicts()
         assert np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(e, oe)
     if ingest == "pipelined":
+        from abstraction_regret_gb300 import native
+
         assert len(r.slices) == 3
-        assert sum(c for _, _, _, c in r.slices) == r.pipe_plan.tasks_l.shape[0]
+        h = r.plan.h_header.numpy()
+        ranges = [(int(h[native.PLAN_SLICES + 2 * k]), int(h[native.PLAN_SLICES + 2 * k + 1]))
+                  for k in range(3)]
+        assert ranges[0][0] == 0
+        assert all(a + c == b for (a, c), (b, _) in zip(ranges, ranges[1:]))
+        assert sum(c for _, c in ranges) == int(h[native.PLAN_LANE_TASKS]) > 0

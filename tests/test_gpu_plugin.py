@@ -44,6 +44,7 @@ def _fresh(name: str):
                                                   PKG / f"{name}.py")
     mod = importlib.util.module_from_spec(spec)
     mod.__package__ = "abstraction_regret_gb300"
+    sys.modules[spec.name] = mod  # dataclasses resolve their annotations through it
     spec.loader.exec_module(mod)
     return mod
 
