@@ -26,7 +26,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import native
+from . import costmodel, native
 
 BITMAP_MAX_WORDS = 8  # thread-per-input bitmaps beyond 512 states scan too many words
 
@@ -85,8 +85,14 @@ def _sm_count() -> int:
 def rule_plan(f: Features, n_inputs: int) -> native.Plan:
     """The rule used before (or instead of) measurement."""
     sms = _sm_count()
-    # Many inputs and a small state set: one thread per input keeps every lane busy.
-    if f.num_words <= BITMAP_MAX_WORDS and n_inputs >= 8 * sms * 32 and not f.uses_any:
+    # Many inputs and a small state set: one thread per input keeps every lane busy, as
+    # long as its sets stay in shared memory (the cost model's residency: otherwise each
+    # symbol moves 4 words of set per state-word through global memory) and its word
+    # scan per symbol stays short.
+    bitmap_ws = costmodel.working_set_traffic_per_symbol(
+        f, costmodel.residency(f, native.TECH_BITMAP, 128))
+    if (f.num_words <= BITMAP_MAX_WORDS and bitmap_ws == 0 and n_inputs >= 8 * sms * 32
+            and not f.uses_any):
         return native.make_plan(native.TECH_BITMAP, block_threads=128, stage=1)
     # Otherwise a warp per input; the sparse list falls back to the dense bitmap itself.
     threads = 128 if n_inputs >= 4 * sms * 4 else 64
@@ -111,19 +117,18 @@ def choose_nfa_plan(dev_nfa, n_inputs: int, persistent: bool = False):
     return rule_plan(f, n_inputs)
 
 
-# Longest input from which a batch goes to the chunked engine: a plain launch simulates
-# each input serially, one dependent L2 round trip (~0.5 us) or more per byte, so an
-# input of 512 bytes already costs it ~250 us, far more than the engine's few extra
-# launches; shorter batches are faster as one plain launch.
-ENGINE_MIN_LONGEST = 512
-
-
-def prefer_engine(dev_nfa, lengths) -> bool:
-    """Run this batch through the chunked engine rather than one plain launch?"""
+def prefer_engine(dev_nfa, lengths, model=None) -> bool:
+    """Run this batch through the chunked engine rather than one plain launch? The cost
+    model's answer (costmodel.py): a plain launch takes at least its longest input's
+    chain of dependent steps; the engine adds planning and three launches but cuts every
+    input into chunks that run in parallel. Only automata with speculative start sets
+    can be chunked."""
     lengths = np.asarray(lengths)
     if lengths.size == 0 or not getattr(dev_nfa, "speculative", False):
         return False
-    return int(lengths.max()) >= ENGINE_MIN_LONGEST
+    f = features(dev_nfa) if hasattr(dev_nfa, "num_sym_edges") else features_of(dev_nfa)
+    m = model or costmodel.DEFAULT
+    return m.predict_engine_ms(f, lengths) < m.predict_plain_ms(f, lengths)
 
 
 def candidate_plans(f: Features) -> list[native.Plan]:

@@ -277,22 +277,138 @@ def c5_pool() -> list:
     return nfas + dfas
 
 
-def c5(rate_per_s: float = 2000.0, n_requests: int = 20000, pool_bytes: int = 1 << 26,
-       automata=None) -> ServingTrace:
-    """Serving trace: Poisson arrivals at ``rate_per_s``, seed 7.
+C5_MAX_REQUEST = 4 << 20
 
-    Request bytes are uniform random, drawn as slices of one shared random pool (a
-    documented economy: 20000 independent draws would be ~7.6 GB of host memory).
+
+def c5(rate_per_s: float = 2000.0, n_requests: int = 20000, pool_bytes: int = 1 << 26,
+       automata=None, variant: str = "literal", walks_per_nfa: int = 4) -> ServingTrace:
+    """Serving trace: Poisson arrivals at ``rate_per_s``, seed 7, lengths log-uniform in
+    64 B..4 MiB, automata drawn uniformly from the pool.
+
+    ``literal``: request bytes are uniform random, drawn as slices of one shared random
+    pool (a documented economy: 20000 independent draws would be ~7.6 GB of host memory);
+    NFA requests then die within a byte or two and DFA requests latch after ~250 bytes.
+    ``live``: an NFA request is a prefix of one of ``walks_per_nfa`` random walks of its
+    automaton (4 MiB each, kept after the uniform pool), so its active set stays alive;
+    DFA requests as in ``literal``. ``sustained``: as ``live`` with every accept bit of
+    every automaton cleared (the reference's latch control), so every offered byte is
+    examined.
     """
-    automata = automata if automata is not None else c5_pool()
+    if variant not in ("literal", "live", "sustained"):
+        raise ValueError(f"unknown c5 variant {variant!r}")
+    automata = list(automata) if automata is not None else c5_pool()
     rng = np.random.default_rng(7)
     gaps = rng.exponential(1.0 / rate_per_s, n_requests)
     arrivals = np.cumsum(gaps) - gaps[0]
     aut_ids = rng.integers(0, len(automata), n_requests)
-    lengths = log_uniform_lengths(rng, n_requests, 64, 4 << 20)
-    pool = uniform_bytes([7, 1], pool_bytes + (4 << 20))
+    lengths = log_uniform_lengths(rng, n_requests, 64, C5_MAX_REQUEST)
     starts = rng.integers(0, pool_bytes, n_requests)
+    uniform = uniform_bytes([7, 1], pool_bytes + C5_MAX_REQUEST)
+    if variant == "literal":
+        return ServingTrace(automata, aut_ids.astype(np.int64), arrivals, uniform, starts,
+                            lengths)
+    nfa_ids = [k for k, a in enumerate(automata) if not hasattr(a, "trans")]
+    parts = [uniform]
+    base = uniform.size
+    walk_start = {}
+    for k in nfa_ids:
+        off = offsets_of(np.full(walks_per_nfa, C5_MAX_REQUEST, dtype=np.int64))
+        parts.append(walk_bytes(automata[k], off, seed=5000 + k))
+        walk_start[k] = base
+        base += int(off[-1])
+    pool = np.concatenate(parts)
+    for i in range(n_requests):
+        k = int(aut_ids[i])
+        if k in walk_start:
+            starts[i] = walk_start[k] + (i % walks_per_nfa) * C5_MAX_REQUEST
+    if variant == "sustained":
+        automata = [without_accepts(a) for a in automata]
     return ServingTrace(automata, aut_ids.astype(np.int64), arrivals, pool, starts, lengths)
 
 
 CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4}
+
+
+# ---- ANML automata ---------------------------------------------------------------------------
+
+
+def _anml_set(rng: np.random.Generator) -> str:
+    """A symbol set as pattern-matching ANML files write them: mostly one byte, else a
+    small range, a negated byte, or any byte."""
+    u = rng.random()
+    if u < 0.70:
+        return f"\\x{int(rng.integers(0, 256)):02x}"
+    if u < 0.90:
+        lo = int(rng.integers(0, 240))
+        return f"[\\x{lo:02x}-\\x{lo + int(rng.integers(1, 16)):02x}]"
+    if u < 0.96:
+        return f"[^\\x{int(rng.integers(0, 256)):02x}]"
+    return "*"
+
+
+def anml_patterns(n_patterns: int, seed: int, min_len: int = 4, max_len: int = 24,
+                  start_of_data: float = 0.1, loop: float = 0.08, branch: float = 0.05) -> str:
+    """A synthetic homogeneous ANML automaton of signature patterns, the shape of the
+    pattern-matching families the reference loads (sparse active sets): each pattern is
+    a chain of ``min_len..max_len`` STEs, started at every position (``all-input``) or
+    only at the start (``start-of-data``), reporting at its last STE; a few STEs keep
+    themselves active (a ``[...]+`` loop) and a few branch to a second successor."""
+    rng = np.random.default_rng(seed)
+    out = ['<anml version="1.0"><automata-network id="patterns">']
+    for p in range(n_patterns):
+        length = int(rng.integers(min_len, max_len + 1))
+        names = [f"p{p}_{k}" for k in range(length)]
+        for k, name in enumerate(names):
+            attrs = f'id="{name}" symbol-set="{_anml_set(rng)}"'
+            if k == 0:
+                attrs += ' start="start-of-data"' if rng.random() < start_of_data \
+                    else ' start="all-input"'
+            body = []
+            if k + 1 < length:
+                body.append(f'<activate-on-match element="{names[k + 1]}"/>')
+                if k + 2 < length and rng.random() < branch:
+                    body.append(f'<activate-on-match element="{names[k + 2]}"/>')
+            else:
+                body.append(f'<report-on-match reportcode="{p}"/>')
+            if rng.random() < loop:
+                body.append(f'<activate-on-match element="{name}"/>')
+            out.append(f'<state-transition-element {attrs}>{"".join(body)}'
+                       f'</state-transition-element>')
+    out.append("</automata-network></anml>")
+    return "\n".join(out)
+
+
+def anml_inputs(nfa, n_inputs: int, length: int, seed: int, plant: float = 0.5) -> list[bytes]:
+    """Inputs for an ANML automaton: uniform bytes, with a random walk of the automaton
+    (from the all-input seeding state) planted at a random position in a ``plant``
+    fraction of them, so that some inputs match."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_inputs):
+        x = rng.integers(0, 256, length, dtype=np.uint8)
+        if length and rng.random() < plant:
+            k = int(rng.integers(1, min(length, 64) + 1))
+            walk = _walk_from(nfa, 1, k, rng)
+            at = int(rng.integers(0, length - walk.size + 1))
+            x[at:at + walk.size] = walk
+        out.append(x.tobytes())
+    return out
+
+
+def _walk_from(nfa, state: int, k: int, rng: np.random.Generator) -> np.ndarray:
+    """Up to k bytes read along symbol edges from ``state`` (ANY edges: a uniform byte),
+    leaving state 1's ANY self-loop on the first step."""
+    rp, tg, sy = nfa.sym_row_ptr, nfa.sym_targets, nfa.sym_symbols
+    out = []
+    s = state
+    for step in range(k):
+        lo, hi = int(rp[s]), int(rp[s + 1])
+        if hi <= lo:
+            break
+        e = int(rng.integers(lo, hi))
+        if step == 0 and s == 1 and hi - lo > 1:
+            e = int(rng.integers(lo + 1, hi))
+        sym = int(sy[e])
+        out.append(int(rng.integers(0, 256)) if sym > 255 else sym)
+        s = int(tg[e])
+    return np.asarray(out, dtype=np.uint8)

@@ -38,6 +38,7 @@ on its own GPU ("replicas only": inputs are independent, nothing is exchanged).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -64,7 +65,7 @@ def parse_args(argv=None):
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline measurement (used for profiling)")
-    ap.add_argument("--extras", default="plain,run_batch,c1,dfa,c4,serving",
+    ap.add_argument("--extras", default="plain,run_batch,refgpu,c1,dfa,c4,serving",
                     help="comma-separated extra sections after the headline")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the c5 serving trace (0: skip the serving section)")
@@ -437,6 +438,8 @@ def main(argv=None) -> int:
             del r2, ex2, b2
     if "run_batch" in sections and rank == 0:
         extras["run_batch_default"] = run_batch_section(batch, flags, lens, steps=3)
+    if "refgpu" in sections and rank == 0:
+        extras["reference_gpu_kernels"] = reference_gpu_section(dev, max(2, args.steps // 4))
     if "c1" in sections and rank == 0:
         extras["c1_plain_nfa"] = c1_section(dev, max(2, args.steps // 2))
     if "c4" in sections and rank == 0:
@@ -553,6 +556,95 @@ def run_batch_section(batch, flags, lens, steps: int = 3) -> dict:
     return {"value": batch.total_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "ms": ms,
             "calls": steps, "path": path, "kernel_ms_result0": float(res[0].kernel_ms),
             "note": "wall clock per call (median), host bytes in, verdicts out"}
+
+
+def reference_gpu_section(dev, steps: int) -> dict:
+    """The reference's own CUDA kernels (built from its sources for sm_103a, oracle/_ref)
+    on the same GPU and workloads: dfa_kernel on c2-sustained and worklist_warp_kernel on
+    c3-sustained and c1-live, launched as its host functions launch them, with int32
+    symbols and offsets; verdicts checked against the oracle."""
+    import torch
+
+    from abstraction_regret_gb300 import workloads as W
+    from abstraction_regret_gb300.packing import pack_accept
+    from oracle import oracle as O
+    from oracle import ref_cuda as R
+
+    try:
+        dfa_img, wl_img = R.Kernels("dfa"), R.Kernels("worklist_global")
+        dfa_fn, wl_fn = dfa_img.fn("dfa_kernel"), wl_img.fn("worklist_warp_kernel")
+    except (OSError, RuntimeError, KeyError) as exc:
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(run, reps):
+        run()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"built_from": "src/gpufsm/backends/cuda/native/{dfa,worklist_global}.cu, nvcc "
+                         "-cubin sm_103a", "input_layout": "int32 symbols, int32 offsets"}
+    b = W.c2("sustained")
+    dfa = b.automata[0]
+    n = b.n_inputs
+    trans = torch.from_numpy(dfa.trans.astype(np.int32)).to(dev)
+    acc = torch.from_numpy(dfa.accept.astype(np.int8)).to(dev)
+    data = torch.from_numpy(b.data).to(dev).to(torch.int32)
+    off = torch.from_numpy(b.offsets.astype(np.int32)).to(dev)
+    res = torch.zeros((2, n), dtype=torch.int32, device=dev)
+    args = R.dfa_kernel_args(trans.data_ptr(), acc.data_ptr(), data.data_ptr(), off.data_ptr(),
+                             n, dfa.num_states, dfa.start_state, res[0].data_ptr(),
+                             res[1].data_ptr())
+    ms = timed(lambda: R.launch(dfa_fn, (n + 255) // 256, 256, args, stream.cuda_stream), steps)
+    of, ol, oe = O.dfa_batch(dfa, b.data, b.offsets)
+    h = res.cpu().numpy()
+    if not (np.array_equal(h[0], of) and np.array_equal(h[1], ol)):
+        raise SystemExit("reference dfa_kernel differs from the oracle on c2-sustained")
+    out["dfa_c2_sustained"] = {"kernel": "dfa_kernel", "ms": ms,
+                               "offered_GBps": b.total_bytes / (ms * 1e-3) / 1e9,
+                               "examined_GBps": int(oe.sum()) / (ms * 1e-3) / 1e9,
+                               "checked": int(n)}
+    del trans, acc, data, off, res
+    for name, batch, reps in (("worklist_warp_c3_sustained", W.c3("sustained"), 1),
+                              ("worklist_warp_c1_live", W.c1("live"), steps)):
+        nfa = batch.automata[0]
+        n = batch.n_inputs
+        nwords = (nfa.num_states + 63) // 64
+        t = lambda a, dt=torch.int32: torch.from_numpy(np.ascontiguousarray(a).astype(  # noqa: E731
+            np.int32 if dt == torch.int32 else np.int64)).to(dev)
+        srp, stg, ssy = t(nfa.sym_row_ptr), t(nfa.sym_targets), t(nfa.sym_symbols)
+        erp, etg = t(nfa.eps_row_ptr), t(nfa.eps_targets)
+        if etg.numel() == 0:
+            etg = torch.zeros(1, dtype=torch.int32, device=dev)
+        words = torch.from_numpy(pack_accept(nfa).view(np.int64)).to(dev)
+        data = torch.from_numpy(batch.data).to(dev).to(torch.int32)
+        off = torch.from_numpy(batch.offsets.astype(np.int32)).to(dev)
+        bufs = torch.zeros((4, n * nwords), dtype=torch.int64, device=dev)
+        res = torch.zeros((2, n), dtype=torch.int32, device=dev)
+        args = R.worklist_warp_args(srp.data_ptr(), stg.data_ptr(), ssy.data_ptr(),
+                                    erp.data_ptr(), etg.data_ptr(), words.data_ptr(),
+                                    data.data_ptr(), off.data_ptr(), n, nfa.start_state,
+                                    int(nfa.uses_any_symbol), nwords, bufs[0].data_ptr(),
+                                    bufs[1].data_ptr(), bufs[2].data_ptr(), bufs[3].data_ptr(),
+                                    res[0].data_ptr(), res[1].data_ptr())
+        ms = timed(lambda: R.launch(wl_fn, (n * 32 + 255) // 256, 256, args,
+                                    stream.cuda_stream), reps)
+        f, l, ex, _ = O.nfa_batch(nfa, batch.data, batch.offsets)
+        h = res.cpu().numpy()
+        if not (np.array_equal(h[0], f) and np.array_equal(h[1], l)):
+            raise SystemExit(f"reference worklist_warp_kernel differs from the oracle ({name})")
+        out[name] = {"kernel": "worklist_warp_kernel", "ms": ms,
+                     "offered_GBps": batch.total_bytes / (ms * 1e-3) / 1e9,
+                     "examined_GBps": int(ex.sum()) / (ms * 1e-3) / 1e9, "checked": int(n)}
+        del srp, stg, ssy, erp, etg, words, data, off, bufs, res
+    return out
 
 
 def c1_section(dev, steps: int) -> dict:
@@ -697,6 +789,40 @@ def serving_section(dev, n_requests: int, slo_ms: float) -> dict:
         out["rates"].append(d)
         del srv
     out["checked"] = {"plain_equal": n_requests, "oracle_sample": int(sample.size)}
+    # live and sustained traces: random-walk NFA requests (and, sustained, every accept
+    # bit cleared), so the simulations examine the bytes instead of dying or latching
+    out["examined_traces"] = {}
+    for variant in ("live", "sustained"):
+        base = W.c5(rate_per_s=1.0, n_requests=n_requests, automata=pool, variant=variant)
+        eng = engine if variant == "live" else PersistentEngine(base.automata, dev)
+        pinned = torch.from_numpy(base.pool).pin_memory()
+        runs, first = [], None
+        for rate in (8000.0, 32000.0, None):
+            # the same requests; only the arrival times scale with the rate
+            tr = dataclasses.replace(base, arrivals=base.arrivals / (rate or 1.0))
+            srv = Server(engine=eng, slots=3, batch_bytes=256 << 20, max_requests=4096,
+                         zero_copy=True)
+            f, l, lat, st = srv.serve(tr, time_scale=1.0 if rate else 0.0, pinned_pool=pinned)
+            if first is None:
+                first = (f, l)
+                for i in sample[:200]:
+                    a, data = base.request(int(i))
+                    want = O.verdicts(base.automata[a], [bytes(data)])[0]
+                    if (int(f[i]), int(l[i])) != (int(want[0]), int(want[1])):
+                        raise SystemExit(f"serving {variant}: request {i} differs from the oracle")
+            elif not (np.array_equal(f, first[0]) and np.array_equal(l, first[1])):
+                raise SystemExit(f"serving {variant} at {rate}/s: verdicts changed")
+            d = st.as_dict()
+            d.update({"rate_per_s": rate if rate else "all at t=0",
+                      "slo_met": bool(st.p99_ms <= slo_ms)})
+            runs.append(d)
+            del srv
+        out["examined_traces"][variant] = {
+            "trace": ("NFA requests: prefixes of random walks of their automaton; DFA "
+                      "requests: uniform bytes" + ("; every accept bit cleared"
+                                                   if variant == "sustained" else "")),
+            "rates": runs, "oracle_sample": 200}
+        del pinned, base
     return out
 
 

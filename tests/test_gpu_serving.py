@@ -67,3 +67,32 @@ def test_plain_per_request_baseline_agrees(setup):
     flags, lens, _, stats = serve_plain(engine, sub, ex)
     assert np.array_equal(flags, want_f[:100]) and np.array_equal(lens, want_l[:100])
     assert stats.batches == 100
+
+
+def test_live_trace_served_alone_and_in_the_mix():
+    """The live trace (random-walk NFA requests, whose sets stay alive for many
+    kilobytes): verdicts and examined bytes equal the oracle's, batched and alone."""
+    pool = W.c5_pool()
+    trace = W.c5(rate_per_s=20000.0, n_requests=400, pool_bytes=1 << 22, automata=pool,
+                 variant="live", walks_per_nfa=2)
+    engine = PersistentEngine(pool)
+    srv = Server(engine=engine, slots=3, batch_bytes=32 << 20, max_requests=256,
+                 zero_copy=True)
+    flags, lens, _, stats = srv.serve(trace, time_scale=0.25)
+    want, examined = [], 0
+    for i in range(len(trace.aut_ids)):
+        a, data = trace.request(i)
+        d, off = O.flatten([bytes(data)])
+        if hasattr(pool[a], "trans"):
+            f, l, e = O.dfa_batch(pool[a], d, off)
+        else:
+            f, l, e, _ = O.nfa_batch(pool[a], d, off)
+        want.append((int(f[0]), int(l[0])))
+        examined += int(e[0])
+    assert list(zip(flags.tolist(), lens.tolist())) == want
+    assert stats.examined_bytes == examined and examined > stats.offered_bytes // 20
+    rng = np.random.default_rng(1)
+    for i in rng.choice(len(trace.aut_ids), 40, replace=False):
+        a, data = trace.request(int(i))
+        f, l, _, _, _ = engine.run_requests([a], [bytes(data)])
+        assert (int(f[0]), int(l[0])) == want[i]
