@@ -125,10 +125,30 @@ __global__ void __launch_bounds__(256) smem_kernel(int64_t iters, uint64_t *sink
         asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
                      : "=r"(x), "=r"(y), "=r"(z), "=r"(w)
                      : "r"(base + (slot & (kSmemVecs - 1)) * 16u));
-        acc ^= x ^ w;
+        acc ^= x ^ y ^ z ^ w;
         slot += 32u;
     }
     sink_if(acc, sink);
+}
+
+// Copy `n_vec` 16-byte vectors from `src` (device memory, or page-locked host memory
+// mapped into the device's address space) to `dst`: every thread streams its vectors
+// with four independent loads in flight.
+__global__ void __launch_bounds__(256) copy16_kernel(uint4 *__restrict__ dst,
+                                                     const uint4 *__restrict__ src,
+                                                     uint64_t n_vec) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = tid;
+    for (; i + 3 * stride < n_vec; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride],
+                    d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n_vec; i += stride) dst[i] = src[i];
 }
 
 int probe_grid(int blocks_per_sm) { return sm_count() * blocks_per_sm; }
@@ -182,6 +202,20 @@ gbfsm_status gbfsm_probe_chase(const uint32_t *next, uint32_t n, int64_t steps, 
                     "gbfsm_probe_chase: a power-of-two entry count, steps >= 1, 1..1024 chains");
     chase_kernel<<<1, chains, 0, static_cast<cudaStream_t>(stream)>>>(next, n - 1, steps, sink);
     GBFSM_LAUNCH_CHECK("chase_kernel launch");
+    return GBFSM_OK;
+}
+
+gbfsm_status gbfsm_probe_copy(void *dst, const void *src, size_t bytes, int32_t blocks_per_sm,
+                              void *stream) {
+    if (!dst || !src || bytes == 0 || (bytes & 15u) != 0 || blocks_per_sm < 1 ||
+        blocks_per_sm > 8)
+        return fail(GBFSM_INVALID_ARG,
+                    "gbfsm_probe_copy: buffers, a multiple of 16 bytes and 1..8 CTAs per SM");
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) != 0)
+        return fail(GBFSM_INVALID_ARG, "gbfsm_probe_copy: buffers not 16-byte aligned");
+    copy16_kernel<<<probe_grid(blocks_per_sm), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<uint4 *>(dst), static_cast<const uint4 *>(src), (uint64_t)(bytes / 16));
+    GBFSM_LAUNCH_CHECK("copy16_kernel launch");
     return GBFSM_OK;
 }
 

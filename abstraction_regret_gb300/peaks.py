@@ -11,7 +11,10 @@ of ``csrc/peaks.cu``, timed with CUDA events (best of several launches after a w
 * ``l2_latency_ns``: one dependent 4-byte L2 load (a pointer chase over a random cycle of
   a 4 MiB table);
 * ``smem_GBps``: bank-conflict-free 16-byte shared-memory loads, 4 CTAs of 256 threads
-  per SM.
+  per SM;
+* ``h2d_*_GBps``: the host link, 256 MiB from page-locked memory: one copy-engine
+  transfer (``dma``), four concurrent ones (``dma4``), and a copy driven by the SMs
+  reading the mapped host buffer (``sm2`` / ``sm8``: 2 or 8 CTAs of 256 threads per SM).
 
     python -m abstraction_regret_gb300.peaks     # prints the figures as one JSON line
 """
@@ -94,10 +97,42 @@ def measure(device=None) -> dict:
                                    "gbfsm_probe_smem"), stream)
         out["smem_GBps"] = sm * blocks * 4096 * iters / (ms * 1e-3) / 1e9
         del buf, d_next
+        # host -> device ingest of 256 MiB from page-locked memory: one copy-engine
+        # transfer, four concurrent transfers of a quarter each, and an SM-driven copy
+        # reading the mapped host buffer over the host link
+        nbytes = 256 << 20
+        h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        h.fill_(7)
+        d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        ms = _best_ms(lambda: d.copy_(h, non_blocking=True), stream, reps=3)
+        out["h2d_dma_GBps"] = nbytes / (ms * 1e-3) / 1e9
+        side = [torch.cuda.Stream(dev) for _ in range(4)]
+        q = nbytes // 4
+
+        def four():
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            for k, st in enumerate(side):
+                st.wait_event(ev)
+                with torch.cuda.stream(st):
+                    d[k * q:(k + 1) * q].copy_(h[k * q:(k + 1) * q], non_blocking=True)
+            for st in side:
+                stream.wait_stream(st)
+
+        ms = _best_ms(four, stream, reps=3)
+        out["h2d_dma4_GBps"] = nbytes / (ms * 1e-3) / 1e9
+        hp = native.device_pointer(h.data_ptr())
+        for blocks in (2, 8):
+            ms = _best_ms(lambda: call(lib.gbfsm_probe_copy(d.data_ptr(), hp, nbytes, blocks, s),
+                                       "gbfsm_probe_copy"), stream, reps=3)
+            out[f"h2d_sm{blocks}_GBps"] = nbytes / (ms * 1e-3) / 1e9
+        del h, d
     out["method"] = ("CUDA events, best of 5 launches after a warm-up: L2 streaming read of "
                      "32 MiB x 16 passes (ld.global.cg); 16-byte random gathers from 1 MiB; "
                      "pointer chase over a 4 MiB random cycle (1 chain, 100k steps); "
-                     "shared-memory 16-byte loads, 4 CTAs x 256 threads per SM")
+                     "shared-memory 16-byte loads, 4 CTAs x 256 threads per SM; host->device "
+                     "256 MiB from pinned memory by copy engines and by an SM copy kernel "
+                     "(best of 3)")
     return out
 
 

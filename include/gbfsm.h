@@ -547,6 +547,12 @@ gbfsm_status gbfsm_probe_gather16(const void *table, size_t table_bytes, int64_t
  * dependent load. */
 gbfsm_status gbfsm_probe_chase(const uint32_t *next, uint32_t n, int64_t steps, int32_t chains,
                                uint64_t *sink, void *stream);
+/* Copy `bytes` (a multiple of 16, both pointers 16-byte aligned) from `src` to `dst` with
+ * blocks_per_sm (1..8) CTAs of 256 threads per SM streaming 16-byte vectors. `src` may be
+ * page-locked host memory mapped into the device (gbfsm_host_device_pointer): the copy is
+ * then driven by the SMs over the host link instead of by a copy engine. */
+gbfsm_status gbfsm_probe_copy(void *dst, const void *src, size_t bytes, int32_t blocks_per_sm,
+                              void *stream);
 /* blocks_per_sm (1..8) CTAs of 256 threads per SM, each thread making `iters` 16-byte
  * bank-conflict-free shared-memory loads: 4096 * iters bytes per CTA. */
 gbfsm_status gbfsm_probe_smem(int64_t iters, int32_t blocks_per_sm, uint64_t *sink, void *stream);
