@@ -553,6 +553,10 @@ gbfsm_status gbfsm_probe_chase(const uint32_t *next, uint32_t n, int64_t steps, 
  * then driven by the SMs over the host link instead of by a copy engine. */
 gbfsm_status gbfsm_probe_copy(void *dst, const void *src, size_t bytes, int32_t blocks_per_sm,
                               void *stream);
+/* Whether the current device reads pageable host memory coherently (no registration):
+ * 0 no, 1 yes, 2 yes through the host's page tables (address translation services);
+ * -1 when the device cannot be asked. A query only: nothing is accessed. */
+int32_t gbfsm_probe_pageable_access(void);
 /* blocks_per_sm (1..8) CTAs of 256 threads per SM, each thread making `iters` 16-byte
  * bank-conflict-free shared-memory loads: 4096 * iters bytes per CTA. */
 gbfsm_status gbfsm_probe_smem(int64_t iters, int32_t blocks_per_sm, uint64_t *sink, void *stream);
