@@ -78,6 +78,9 @@ gbfsm_status launch_lanes(const gbfsm_automaton *table, int32_t n_automata,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream);
 size_t batch_plan_scratch_bytes(int32_t n_inputs);
+gbfsm_status launch_gather_inputs(const uint64_t *src, const int64_t *offsets, int32_t n,
+                                  uint8_t *dst, cudaStream_t stream);
+int32_t pageable_access();
 gbfsm_status launch_batch_plan(const gbfsm_batch_plan_args &args, cudaStream_t stream);
 size_t persistent_workspace_bytes(int32_t max_words, const gbfsm_plan &p);
 int32_t persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan &p);

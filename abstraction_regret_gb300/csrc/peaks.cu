@@ -219,21 +219,6 @@ gbfsm_status gbfsm_probe_copy(void *dst, const void *src, size_t bytes, int32_t 
     return GBFSM_OK;
 }
 
-int32_t gbfsm_probe_pageable_access(void) {
-    int dev = 0, v = 0, host_tables = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
-        cudaGetLastError();
-        return -1;
-    }
-    if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
-                               dev) != cudaSuccess) {
-        cudaGetLastError();
-        host_tables = 0;
-    }
-    return v ? (host_tables ? 2 : 1) : 0;
-}
-
 gbfsm_status gbfsm_probe_smem(int64_t iters, int32_t blocks_per_sm, uint64_t *sink, void *stream) {
     if (!sink || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 8)
         return fail(GBFSM_INVALID_ARG, "gbfsm_probe_smem: bad iterations or blocks per SM");

@@ -214,7 +214,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_probe_chase": (ctypes.c_int, [_vp, ctypes.c_uint32, _i64, _i32, _vp, _vp]),
     "gbfsm_probe_smem": (ctypes.c_int, [_i64, _i32, _vp, _vp]),
     "gbfsm_probe_copy": (ctypes.c_int, [_vp, _vp, _sz, _i32, _vp]),
-    "gbfsm_probe_pageable_access": (_i32, []),
+    "gbfsm_pageable_access": (_i32, []),
+    "gbfsm_gather_inputs": (ctypes.c_int, [_vp, _vp, _i32, _vp, _vp]),
 }
 
 ABI_VERSION = 2

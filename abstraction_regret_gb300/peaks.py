@@ -127,7 +127,7 @@ def measure(device=None) -> dict:
                                        "gbfsm_probe_copy"), stream, reps=3)
             out[f"h2d_sm{blocks}_GBps"] = nbytes / (ms * 1e-3) / 1e9
         del h, d
-        out["pageable_access"] = int(lib.gbfsm_probe_pageable_access())
+        out["pageable_access"] = int(lib.gbfsm_pageable_access())
     out["method"] = ("CUDA events, best of 5 launches after a warm-up: L2 streaming read of "
                      "32 MiB x 16 passes (ld.global.cg); 16-byte random gathers from 1 MiB; "
                      "pointer chase over a 4 MiB random cycle (1 chain, 100k steps); "

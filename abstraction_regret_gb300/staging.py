@@ -1,18 +1,38 @@
-"""Host->device staging of byte batches through reusable pinned buffers.
+"""Host->device staging of byte batches.
 
 The reference widens every input byte to an int32 and copies the batch synchronously
 from pageable memory on every call (src/gpufsm/core/packing.py:35-63,
-native/include/common.cuh:150-159). Here a batch is packed once into a pinned uint8
-buffer (1 byte per symbol, int64 offsets, 16-byte padding) and copied with
-``cudaMemcpyAsync`` on the caller's stream; buffers grow geometrically and are reused.
+native/include/common.cuh:150-159). Here a batch becomes one uint8 device buffer (1 byte
+per symbol, int64 offsets, 16-byte padding) in one of two ways:
+
+* on a device that reads pageable host memory coherently (GB300 over NVLink-C2C,
+  ``gbfsm_pageable_access``), and for batches of at least ``GATHER_MIN_BYTES``, the GPU
+  copies every input from the caller's own buffer (the ``bytes`` objects themselves):
+  only their addresses and the offsets cross the link as a table, the bytes are read by
+  ``gbfsm_gather_inputs``, and nothing is packed on the host;
+* otherwise the batch is packed into a pinned buffer and copied with
+  ``cudaMemcpyAsync``.
+
+Buffers grow geometrically and are reused.
 """
 
 from __future__ import annotations
+
+import ctypes
 
 import numpy as np
 import torch
 
 from .packing import PAD
+
+GATHER_MIN_BYTES = 1 << 20  # smaller batches: packing costs less than the extra launch
+
+
+def _address(b) -> int:
+    """Address of the bytes of a buffer-protocol object (its own storage, no copy)."""
+    if isinstance(b, bytes):
+        return ctypes.cast(b, ctypes.c_void_p).value or 0
+    return int(np.frombuffer(b, dtype=np.uint8).ctypes.data)
 
 
 def _grow(cap: int, need: int) -> int:
@@ -29,11 +49,28 @@ class Staging:
     executors synchronise on their results before returning, which guarantees it).
     """
 
-    def __init__(self, device: torch.device) -> None:
+    def __init__(self, device: torch.device, gather: bool | None = None) -> None:
+        """``gather``: None = read the inputs in place when the device can, False = always
+        pack, True = always read in place (the device must read pageable memory)."""
         self.device = device
         self._h_data = self._d_data = None
         self._h_off = self._d_off = None
+        self._h_ptr = self._d_ptr = None
         self._cap_data = self._cap_off = 0
+        self.gather = gather
+        self._pageable = None
+        self.last_path = None
+
+    def _can_gather(self) -> bool:
+        if self._pageable is None:
+            from . import native
+
+            with torch.cuda.device(self.device):
+                self._pageable = native.lib().gbfsm_pageable_access() > 0
+            if self.gather and not self._pageable:
+                raise ValueError("this device does not read pageable host memory: inputs "
+                                 "cannot be gathered in place")
+        return self._pageable if self.gather is None else bool(self.gather)
 
     def _ensure(self, nbytes: int, n_off: int) -> None:
         if nbytes > self._cap_data:
@@ -44,6 +81,8 @@ class Staging:
             self._cap_off = _grow(self._cap_off, n_off)
             self._h_off = torch.empty(self._cap_off, dtype=torch.int64, pin_memory=True)
             self._d_off = torch.empty(self._cap_off, dtype=torch.int64, device=self.device)
+            self._h_ptr = torch.empty(self._cap_off, dtype=torch.int64, pin_memory=True)
+            self._d_ptr = torch.empty(self._cap_off, dtype=torch.int64, device=self.device)
 
     def put(self, inputs, stream: torch.cuda.Stream):
         """Pack ``inputs`` (bytes-like objects) and start their copy on ``stream``.
@@ -60,6 +99,25 @@ class Staging:
         h_off[0] = 0
         if n:
             np.cumsum(lens, out=h_off[1:])
+        if n and total >= GATHER_MIN_BYTES and self._can_gather():
+            # the GPU reads each input where it lies; the caller keeps ``inputs`` alive
+            # until the stream has passed this copy (the executors synchronise first)
+            h_ptr = self._h_ptr.numpy()
+            for i, b in enumerate(inputs):
+                h_ptr[i] = _address(b)
+            from . import native
+
+            with torch.cuda.stream(stream):
+                self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
+                self._d_ptr[:n].copy_(self._h_ptr[:n], non_blocking=True)
+                if padded > total:
+                    self._d_data[total:padded].zero_()
+                native.check(native.lib().gbfsm_gather_inputs(
+                    self._d_ptr.data_ptr(), self._d_off.data_ptr(), n,
+                    self._d_data.data_ptr(), stream.cuda_stream), "gbfsm_gather_inputs")
+            self.last_path = "gather"
+            return self._d_data[:padded], self._d_off[: n + 1], h_off, total
+        self.last_path = "pack"
         h_data = self._h_data.numpy()
         pos = 0
         for b in inputs:

@@ -346,6 +346,23 @@ gbfsm_status gbfsm_persistent_run(const gbfsm_automaton *table, int32_t n_automa
  * counterpart in the reference (which copies every input, common.cuh:150-159). */
 gbfsm_status gbfsm_host_device_pointer(void *host, void **device);
 
+/* Whether the current device reads pageable host memory coherently, without registering
+ * it: 0 no, 1 yes, 2 yes through the host's page tables (address translation services, as
+ * GB300 over NVLink-C2C); -1 when the device cannot be asked. A query: nothing is
+ * accessed. No counterpart in the reference. */
+int32_t gbfsm_pageable_access(void);
+
+/* Copy n_inputs inputs into the contiguous device layout of a batch: input i, the bytes
+ * src_ptrs[i] .. src_ptrs[i] + (offsets[i+1] - offsets[i]), goes to
+ * dst[offsets[i] .. offsets[i+1]). src_ptrs (uint64 addresses) and offsets are device
+ * arrays; dst is device memory of at least offsets[n_inputs] rounded up to 16 bytes. A
+ * source may be device memory, page-locked host memory mapped into the device, or, where
+ * gbfsm_pageable_access() > 0, any pageable host memory; it is read in aligned 16-byte
+ * blocks that each hold at least one of its bytes. One warp per input; stream-ordered.
+ * No counterpart in the reference (which packs and copies every batch on the host). */
+gbfsm_status gbfsm_gather_inputs(const uint64_t *src_ptrs, const int64_t *offsets,
+                                 int32_t n_inputs, uint8_t *dst, void *stream);
+
 /* Resident warps per SM of the lane launch on the current device (0 when it cannot run):
  * a batch whose LANES tasks fit sm_count times this runs in one wave. No counterpart in
  * the reference. */
@@ -553,10 +570,6 @@ gbfsm_status gbfsm_probe_chase(const uint32_t *next, uint32_t n, int64_t steps, 
  * then driven by the SMs over the host link instead of by a copy engine. */
 gbfsm_status gbfsm_probe_copy(void *dst, const void *src, size_t bytes, int32_t blocks_per_sm,
                               void *stream);
-/* Whether the current device reads pageable host memory coherently (no registration):
- * 0 no, 1 yes, 2 yes through the host's page tables (address translation services);
- * -1 when the device cannot be asked. A query only: nothing is accessed. */
-int32_t gbfsm_probe_pageable_access(void);
 /* blocks_per_sm (1..8) CTAs of 256 threads per SM, each thread making `iters` 16-byte
  * bank-conflict-free shared-memory loads: 4096 * iters bytes per CTA. */
 gbfsm_status gbfsm_probe_smem(int64_t iters, int32_t blocks_per_sm, uint64_t *sink, void *stream);
