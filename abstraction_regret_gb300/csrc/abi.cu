@@ -284,8 +284,11 @@ gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *a, void *stream) {
     if (a->min_chunk < 64)
         return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: min_chunk %d below 64", a->min_chunk);
     if (a->cap_chunks < 1 || a->cap_lane_tasks < 0 || a->cap_persist_tasks < 0 ||
-        a->cap_fixup_tasks < 0)
+        a->cap_fixup_tasks < 0 || a->cap_dfa_chunk_tasks < 0 || a->cap_dfa_fixup_tasks < 0)
         return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: negative capacity");
+    if (a->aut_dfa_chunk && (!a->tasks_dfa_chunk || !a->tasks_dfa_fixup))
+        return fail(GBFSM_INVALID_ARG,
+                    "gbfsm_batch_plan: aut_dfa_chunk needs tasks_dfa_chunk and tasks_dfa_fixup");
     if (a->n_slices > GBFSM_PLAN_MAX_SLICES)
         return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: more than %d slices",
                     GBFSM_PLAN_MAX_SLICES);

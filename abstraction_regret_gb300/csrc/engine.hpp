@@ -82,6 +82,15 @@ gbfsm_status launch_gather_inputs(const uint64_t *src, const int64_t *offsets, i
                                   uint8_t *dst, cudaStream_t stream);
 int32_t pageable_access();
 gbfsm_status launch_batch_plan(const gbfsm_batch_plan_args &args, cudaStream_t stream);
+
+// DFA_CHUNK / DFA_FIXUP tasks (dfa_chunks.cu).
+gbfsm_status launch_dfa_chunks(const gbfsm_automaton *table, int32_t n_automata,
+                               const gbfsm_task *tasks, int32_t max_tasks,
+                               const int32_t *task_count, const uint8_t *data,
+                               const int64_t *offsets, const int64_t *ends,
+                               const gbfsm_chunk_io &chunk_io, int32_t max_states,
+                               int32_t *flags, int32_t *lens, int32_t *examined,
+                               int32_t *latch, cudaStream_t stream);
 size_t persistent_workspace_bytes(int32_t max_words, const gbfsm_plan &p);
 int32_t persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan &p);
 gbfsm_status launch_nfa_layout(int32_t n, const int32_t *srp, const int32_t *stg,

@@ -12,7 +12,8 @@
 //      resident warp of the persistent launch; with slices, the lane size of slice k of
 //      P is scaled by 1 - shrink * k / P;
 //   3. count each input's chunks, exclusive-scan the counts over the inputs in index
-//      order (lane chunks first, then warp chunks), place the FIXUP tasks in input
+//      order (lane chunks first, then warp chunks, then the chunks of long DFA inputs),
+//      place the FIXUP and DFA_FIXUP tasks in input
 //      order, and histogram the persistent launch's tasks by log2 of their work (WHOLE
 //      NFA inputs, warp chunks, groups of 32 DFA inputs) so that they can be queued
 //      longest first, bucket by bucket;
@@ -174,7 +175,7 @@ __device__ __forceinline__ int64_t lane_size(const gbfsm_batch_plan_args &a, int
 
 __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_plan_args a,
                                                                  PlanScratch s) {
-    __shared__ int64_t red[4 * 32 + 1];
+    __shared__ int64_t red[6 * 32 + 1];
     __shared__ int32_t h_work[kBuckets], h_dfa[kBuckets], h_grp[kBuckets];
     __shared__ int32_t bad;
     const int32_t n = a.n_inputs;
@@ -253,11 +254,24 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
     }
 
     // 3. per-input counts, scans and bucket histograms
-    int64_t v[4] = {0, 0, 0, 0};  // lane chunks, warp chunks, split inputs, whole NFA inputs
+    // lane chunks, warp chunks, split NFA inputs, whole NFA inputs, DFA chunks, chunked
+    // DFA inputs
+    int64_t v[6] = {0, 0, 0, 0, 0, 0};
     for (int32_t i = lo; i < hi; ++i) {
         const int32_t c = s.cls[i];
         const int64_t len = input_len(a, i);
         int64_t cnt = 0;
+        const int64_t dfa_chunk = (c == GBFSM_PLAN_DFA && a.aut_dfa_chunk)
+                                      ? (int64_t)a.aut_dfa_chunk[a.aut_ids ? a.aut_ids[i] : 0]
+                                      : 0;
+        if (c == GBFSM_PLAN_DFA && dfa_chunk > 0 && len >= 2 * dfa_chunk) {
+            // a long DFA input: cut into chunks walked in parallel (DFA_CHUNK tasks)
+            cnt = chunks_of(len, dfa_chunk);
+            v[4] += cnt;
+            v[5] += 1;
+            s.cnt[i] = (int32_t)cnt;
+            continue;
+        }
         if (c == GBFSM_PLAN_NFA_LANES) {
             cnt = chunks_of(len, lane_size(a, lane_base, i));
             v[0] += cnt;
@@ -274,16 +288,22 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
         s.cnt[i] = (int32_t)cnt;
         if (cnt > 0) v[2] += 1;
     }
-    int64_t tot[4];
-    int64_t ex[4] = {v[0], v[1], v[2], v[3]};
-    block_scan<4>(ex, tot, red);
+    int64_t tot[6];
+    int64_t ex[6] = {v[0], v[1], v[2], v[3], v[4], v[5]};
+    block_scan<6>(ex, tot, red);
     const int64_t n_lane = tot[0], n_warp = tot[1], n_split = tot[2], n_whole = tot[3];
-    const int64_t n_chunks = n_lane + n_warp;
+    const int64_t n_dfa_chunks = tot[4], n_dfa_split = tot[5];
+    const int64_t n_chunks = n_lane + n_warp + n_dfa_chunks;
     for (int32_t i = lo; i < hi; ++i) {
         const int32_t c = s.cls[i];
         s.lpre[i] = (int32_t)ex[0];
         const int32_t cnt = s.cnt[i];
-        if (cnt > 0) {
+        if (cnt > 0 && c == GBFSM_PLAN_DFA) {
+            s.first[i] = (int32_t)(n_lane + n_warp + ex[4]);
+            ex[4] += cnt;
+            s.fix[i] = (int32_t)ex[5];
+            ex[5] += 1;
+        } else if (cnt > 0) {
             if (c == GBFSM_PLAN_NFA_LANES) {
                 s.first[i] = (int32_t)ex[0];
                 ex[0] += cnt;
@@ -320,7 +340,11 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
             }
             const int64_t n_lane_tasks = (n_lane + kLaneGroup - 1) / kLaneGroup;
             const bool over = n_chunks + 1 > a.cap_chunks || n_lane_tasks > a.cap_lane_tasks ||
-                              t > a.cap_persist_tasks || n_split > a.cap_fixup_tasks || bad;
+                              t > a.cap_persist_tasks || n_split > a.cap_fixup_tasks ||
+                              n_dfa_chunks > a.cap_dfa_chunk_tasks ||
+                              n_dfa_split > a.cap_dfa_fixup_tasks ||
+                              (n_dfa_chunks > 0 && (!a.tasks_dfa_chunk || !a.tasks_dfa_fixup)) ||
+                              bad;
             int32_t *h = a.header;
             h[GBFSM_PLAN_STATUS] = bad ? 2 : over ? 1 : 0;
             h[GBFSM_PLAN_LANE_CHUNKS] = over ? 0 : (int32_t)n_lane;
@@ -334,6 +358,8 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
             h[GBFSM_PLAN_OVERFLOW] = 0;
             h[GBFSM_PLAN_WHOLE] = (int32_t)n_whole;
             h[GBFSM_PLAN_DFA_INPUTS] = d;
+            h[GBFSM_PLAN_DFA_CHUNKS] = over ? 0 : (int32_t)n_dfa_chunks;
+            h[GBFSM_PLAN_DFA_FIXUPS] = over ? 0 : (int32_t)n_dfa_split;
             // lane task range of each slice: task t waits for the slice holding the input
             // of its last chunk, min(32 t + 31, n_lane - 1)
             const int ns = a.n_slices > 1 ? a.n_slices : 1;
@@ -374,7 +400,24 @@ __global__ void __launch_bounds__(256) plan_fill_kernel(gbfsm_batch_plan_args a,
         const int64_t st = a.offsets[i];
         const int64_t len = input_len(a, i);
         const int32_t cnt = s.cnt[i];
-        if (cnt > 0) {
+        if (cnt > 0 && c == GBFSM_PLAN_DFA) {  // a long DFA input: chunks walked by warps
+            const int32_t f = s.first[i];
+            const int32_t base = n_chunks - h[GBFSM_PLAN_DFA_CHUNKS];
+            for (int32_t k = (int32_t)lane; k < cnt; k += 32) {
+                gbfsm_chunk ch;
+                ch.input = i;
+                ch.index = k;
+                ch.begin = st + (int64_t)k * len / cnt;
+                ch.end = st + (int64_t)(k + 1) * len / cnt;
+                a.chunks[f + k] = ch;
+                a.tasks_dfa_chunk[f - base + k] =
+                    gbfsm_task{aut, f + k, 1, GBFSM_TASK_DFA_CHUNK};
+            }
+            if (lane == 0) {
+                a.tasks_dfa_fixup[s.fix[i]] = gbfsm_task{aut, f, cnt, GBFSM_TASK_DFA_FIXUP};
+                if (a.dfa_latch) a.dfa_latch[i] = INT32_MAX;
+            }
+        } else if (cnt > 0) {
             const int32_t f = s.first[i];
             int32_t slot0 = 0;
             if (c != GBFSM_PLAN_NFA_LANES && lane == 0)

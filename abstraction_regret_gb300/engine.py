@@ -54,6 +54,24 @@ LANE_PAIR_MEAN = 32.0
 # resident warps per SM of the lane launch when the device is not asked (128-thread
 # CTAs, 8 per SM: csrc/lanes.cu)
 LANE_WARPS_PER_SM = 32
+# DFA chunking (csrc/dfa_chunks.cu): the largest DFA whose inputs are chunked (2-byte
+# table entries), the shortest DFA chunk, and the chunk and overlap lengths per state
+DFA_CHUNK_MAX_STATES = 32768
+DFA_CHUNK_MIN = 64 << 10
+DFA_CHUNK_FLOOR = 4096  # the shortest DFA chunk a caller may ask for
+DFA_CHUNK_PER_STATE = 8
+DFA_OVERLAP_PER_STATE = 12
+
+
+def dfa_chunk_length(num_states: int) -> int:
+    """Chunk length for the long inputs of a DFA of ``num_states`` states (a multiple of
+    64 bytes): its set of all states must usually collapse well inside one chunk."""
+    return -(-max(DFA_CHUNK_MIN, DFA_CHUNK_PER_STATE * int(num_states)) // 64) * 64
+
+
+def dfa_overlap_bytes(num_states: int) -> int:
+    """Most bytes a DFA chunk's exact walk continues into the next chunk."""
+    return DFA_OVERLAP_PER_STATE * int(num_states)
 
 
 @dataclass
@@ -183,17 +201,22 @@ class DevicePlan:
             factor = 1.25 / (1.0 - self.shrink)
             cap = int(factor * (LANE_GROUP * lw + int(total_bytes) // (1 << 20) + n)) + \
                 8 * pw + 2 * n + 64
-        self.cap_chunks = cap
+        self.cap_dfa_chunks, self.cap_dfa_fixup = self.dfa_caps(engine, n, total_bytes)
         self.cap_lanes = cap // LANE_GROUP + 2
         self.cap_persist = n + cap
         self.cap_fixup = n
+        cap += self.cap_dfa_chunks
+        self.cap_chunks = cap
         i32 = torch.int32
         self.chunks = torch.empty(cap * 24, dtype=torch.uint8, device=dev)
         self.records = torch.empty(cap * native.CHUNK_RECORD_BYTES, dtype=torch.uint8, device=dev)
         self.overflow = torch.empty(cap * 4, dtype=i32, device=dev)
-        self.tasks = torch.empty((self.cap_lanes + self.cap_persist + self.cap_fixup) * 4,
+        self.tasks = torch.empty((self.cap_lanes + self.cap_persist + self.cap_fixup +
+                                  self.cap_dfa_chunks + self.cap_dfa_fixup) * 4,
                                  dtype=i32, device=dev)
         self.input_ids = torch.empty(n, dtype=i32, device=dev)
+        # per input: the lowest chunk index that found an accept (chunked DFA inputs)
+        self.dfa_latch = torch.empty(n if self.cap_dfa_chunks else 1, dtype=i32, device=dev)
         self.header = torch.zeros(native.PLAN_HEADER_WORDS, dtype=i32, device=dev)
         self.h_header = torch.zeros(native.PLAN_HEADER_WORDS, dtype=i32, pin_memory=True)
         lib = native.lib()
@@ -203,6 +226,18 @@ class DevicePlan:
         self.tasks_lanes = base
         self.tasks_persist = base + self.cap_lanes * 16
         self.tasks_fixup = base + (self.cap_lanes + self.cap_persist) * 16
+        self.tasks_dfa_chunk = self.tasks_fixup + self.cap_fixup * 16
+        self.tasks_dfa_fixup = self.tasks_dfa_chunk + self.cap_dfa_chunks * 16
+
+    @staticmethod
+    def dfa_caps(engine: PersistentEngine, n: int, total_bytes: int) -> tuple[int, int]:
+        """Capacities for DFA chunks and DFA fix-ups: an input is chunked when it holds
+        at least two chunks of its DFA, so it has at most 1.5 x its bytes / chunk chunks."""
+        if engine.aut_dfa_chunk is None:
+            return 0, 0
+        c = engine.min_dfa_chunk
+        return (3 * int(total_bytes) // (2 * c) + 2,
+                min(int(n), int(total_bytes) // (2 * c)) + 1)
 
     @staticmethod
     def device_bytes(engine: PersistentEngine, n_inputs: int, total_bytes: int) -> int:
@@ -211,7 +246,9 @@ class DevicePlan:
         n = max(int(n_inputs), 1)
         cap = int(1.25 * (LANE_GROUP * lw + int(total_bytes) // (1 << 20) + n)) + \
             8 * engine.resident_warps + 2 * n + 64
-        return cap * (24 + native.CHUNK_RECORD_BYTES + 16 + 16) + n * 64
+        dc, df = DevicePlan.dfa_caps(engine, n, total_bytes)
+        return (cap + dc) * (24 + native.CHUNK_RECORD_BYTES + 16 + 16) + (dc + df) * 16 + \
+            n * (68 if dc else 64)
 
     def _hdr(self, word: int) -> int:
         return self.header.data_ptr() + 4 * word
@@ -230,6 +267,13 @@ class DevicePlan:
         a.ends = d_ends.data_ptr() if d_ends is not None else None
         a.aut_ids = d_aut.data_ptr() if d_aut is not None else None
         a.aut_class = eng.aut_class.data_ptr()
+        if eng.aut_dfa_chunk is not None:
+            a.aut_dfa_chunk = eng.aut_dfa_chunk.data_ptr()
+            a.tasks_dfa_chunk = self.tasks_dfa_chunk
+            a.tasks_dfa_fixup = self.tasks_dfa_fixup
+            a.dfa_latch = self.dfa_latch.data_ptr()
+        a.cap_dfa_chunk_tasks = self.cap_dfa_chunks
+        a.cap_dfa_fixup_tasks = self.cap_dfa_fixup
         a.lane_warps = eng.sm_count * eng.lane_warps_per_sm
         a.persist_warps = eng.resident_warps
         a.min_chunk = MIN_CHUNK
@@ -268,7 +312,8 @@ class DevicePlan:
 
     def launch(self, data_ptr: int, d_off, d_ends, d_flags, d_lens, d_examined, stream,
                workspace=None, phases: dict | None = None, lane_slices=None) -> int:
-        """Enqueue the four launches of a planned batch; returns their number.
+        """Enqueue the launches of a planned batch (four, six when the pool chunks long DFA
+        inputs); returns their number.
         ``lane_slices``: ``[(side stream, ready event)]`` per slice (pipelined ingest);
         slice k's lane tasks run on its side stream once its event has fired."""
         eng = self.engine
@@ -313,6 +358,23 @@ class DevicePlan:
             mark("lanes")
             launches += 1
 
+        def dfa_chunks(name, tasks_ptr, max_tasks, count_word):
+            mark(name)
+            st = lib.gbfsm_dfa_chunks_run(
+                table, n_aut, tasks_ptr, int(max_tasks), self._hdr(count_word), data_ptr,
+                d_off.data_ptr(), d_ends.data_ptr() if d_ends is not None else None,
+                ctypes.byref(io), eng.dfa_max_states, d_flags.data_ptr(), d_lens.data_ptr(),
+                d_examined.data_ptr() if d_examined is not None else None,
+                self.dfa_latch.data_ptr(), stream.cuda_stream)
+            native.check(st, "gbfsm_dfa_chunks_run")
+            mark(name)
+
+        chunked_dfa = eng.aut_dfa_chunk is not None and self.cap_dfa_chunks > 0
+        if chunked_dfa:
+            dfa_chunks("dfa_chunks", self.tasks_dfa_chunk, self.cap_dfa_chunks,
+                       native.PLAN_DFA_CHUNKS)
+            launches += 1
+
         def persist(name, tasks_ptr, max_tasks, count_word):
             mark(name)
             cio = self.chunk_io(count_word)
@@ -329,6 +391,10 @@ class DevicePlan:
         persist("persistent", self.tasks_persist, self.cap_persist, native.PLAN_PERSIST_TASKS)
         persist("overflow", self.overflow.data_ptr(), self.cap_chunks, native.PLAN_OVERFLOW)
         persist("fixup", self.tasks_fixup, self.cap_fixup, native.PLAN_FIXUP_TASKS)
+        if chunked_dfa:
+            dfa_chunks("dfa_fixup", self.tasks_dfa_fixup, self.cap_dfa_fixup,
+                       native.PLAN_DFA_FIXUPS)
+            launches += 1
         return launches + 3
 
     def fetch_header(self, stream) -> None:
@@ -351,8 +417,11 @@ class PersistentEngine:
     def __init__(self, automata, device=None, choices=None, block_threads: int = 256,
                  list_capacity: int | None = None, ctas_per_sm: int = 0,
                  chunk_bytes: int | None = 0, lane_pair_mean: float = LANE_PAIR_MEAN,
-                 resident=None) -> None:
+                 resident=None, dfa_chunk_bytes: int | None = None) -> None:
         """``chunk_bytes``: 0 = chosen per batch, None = never chunk, else a fixed size.
+        ``dfa_chunk_bytes``: chunk length of long DFA inputs; None = from each DFA's size
+        (dfa_chunk_length()), 0 = DFA inputs always run whole, else this length (rounded up
+        to 64 bytes, at least DFA_CHUNK_FLOOR) for every DFA.
         ``lane_pair_mean``: largest mean two-byte superset for one-lane-per-chunk tasks.
         ``resident``: device layouts already built for ``automata`` (DeviceNFA /
         DeviceDFA, same order), shared instead of built again."""
@@ -392,6 +461,21 @@ class PersistentEngine:
             self.ws_bytes = int(lib.gbfsm_persistent_workspace_bytes(self.max_words,
                                                                      ctypes.byref(self.plan)))
             self.workspace = torch.zeros(self.ws_bytes, dtype=torch.uint8, device=self.device)
+            # long DFA inputs are cut into chunks walked in parallel (DFA_CHUNK tasks): a
+            # chunk of an n-state DFA spans max(64 KiB, 8n) bytes, and its exact walk
+            # continues into the next chunk until it passes that chunk's collapse (about
+            # 2n bytes in for a random DFA), for at most 12n bytes
+            dfa_chunk = [0] * len(self.automata)
+            if chunk_bytes is not None and dfa_chunk_bytes != 0:
+                for i, (d, k) in enumerate(zip(self.dev, self.kinds)):
+                    if k is Kind.DFA and d.entry_bytes == 2 and \
+                            d.num_states <= DFA_CHUNK_MAX_STATES:
+                        dfa_chunk[i] = (dfa_chunk_length(d.num_states) if dfa_chunk_bytes is None
+                                        else -(-max(DFA_CHUNK_FLOOR, int(dfa_chunk_bytes))
+                                               // 64) * 64)
+            self.dfa_chunk = dfa_chunk
+            self.dfa_max_states = max([d.num_states for d, c in zip(self.dev, dfa_chunk) if c]
+                                      or [0])
             table = (native.Automaton * len(self.automata))()
             for i, (d, k, c) in enumerate(zip(self.dev, self.kinds, choices)):
                 if k is Kind.NFA:
@@ -402,6 +486,7 @@ class PersistentEngine:
                 else:
                     table[i].kind = 1
                     table[i].dfa = d.desc
+                    table[i].dfa_overlap = dfa_overlap_bytes(d.num_states) if dfa_chunk[i] else 0
             raw = np.frombuffer(bytes(table), dtype=np.uint8).copy()
             self.table = torch.from_numpy(raw).to(self.device)
             props = torch.cuda.get_device_properties(self.device)
@@ -424,6 +509,9 @@ class PersistentEngine:
             else:
                 cls.append(native.PLAN_NFA_WHOLE)
         self.aut_class = torch.tensor(cls, dtype=torch.int32, device=self.device)
+        self.aut_dfa_chunk = (torch.tensor(self.dfa_chunk, dtype=torch.int32, device=self.device)
+                              if any(self.dfa_chunk) else None)
+        self.min_dfa_chunk = min([c for c in self.dfa_chunk if c] or [0])
         self.fixed_chunk = -1 if chunk_bytes is None else max(0, int(chunk_bytes))
         if self.fixed_chunk > 0:
             self.fixed_chunk = max(self.fixed_chunk, MIN_CHUNK)
@@ -939,7 +1027,9 @@ class GraphRunner:
                 "chunks": int(h[native.PLAN_CHUNKS]),
                 "lane_tasks": int(h[native.PLAN_LANE_TASKS]),
                 "persistent_tasks": int(h[native.PLAN_PERSIST_TASKS]),
-                "fixup_tasks": int(h[native.PLAN_FIXUP_TASKS])}
+                "fixup_tasks": int(h[native.PLAN_FIXUP_TASKS]),
+                "dfa_chunks": int(h[native.PLAN_DFA_CHUNKS]),
+                "dfa_fixups": int(h[native.PLAN_DFA_FIXUPS])}
 
     def verdicts(self):
         """(flags, lens, examined) of the last replay, once it has finished."""

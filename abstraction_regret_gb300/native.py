@@ -103,7 +103,7 @@ class Automaton(ctypes.Structure):
         ("kind", ctypes.c_int32),
         ("technique", ctypes.c_int32),
         ("list_capacity", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("dfa_overlap", ctypes.c_int32),
         ("nfa", NfaDev),
         ("dfa", DfaDev),
     ]
@@ -134,14 +134,18 @@ class BatchPlanArgs(ctypes.Structure):
         ("n_inputs", ctypes.c_int32), ("n_automata", ctypes.c_int32),
         ("offsets", ctypes.c_void_p), ("ends", ctypes.c_void_p),
         ("aut_ids", ctypes.c_void_p), ("aut_class", ctypes.c_void_p),
+        ("aut_dfa_chunk", ctypes.c_void_p),
         ("lane_warps", ctypes.c_int32), ("persist_warps", ctypes.c_int32),
         ("min_chunk", ctypes.c_int32), ("fixed_chunk", ctypes.c_int32),
         ("n_slices", ctypes.c_int32), ("shrink", ctypes.c_float),
         ("slice_first", ctypes.c_int32 * (PLAN_MAX_SLICES + 1)),
         ("cap_chunks", ctypes.c_int32), ("cap_lane_tasks", ctypes.c_int32),
         ("cap_persist_tasks", ctypes.c_int32), ("cap_fixup_tasks", ctypes.c_int32),
+        ("cap_dfa_chunk_tasks", ctypes.c_int32), ("cap_dfa_fixup_tasks", ctypes.c_int32),
         ("chunks", ctypes.c_void_p), ("tasks_lanes", ctypes.c_void_p),
         ("tasks_persist", ctypes.c_void_p), ("tasks_fixup", ctypes.c_void_p),
+        ("tasks_dfa_chunk", ctypes.c_void_p), ("tasks_dfa_fixup", ctypes.c_void_p),
+        ("dfa_latch", ctypes.c_void_p),
         ("input_ids", ctypes.c_void_p), ("header", ctypes.c_void_p),
         ("scratch", ctypes.c_void_p),
     ]
@@ -152,10 +156,11 @@ PLAN_NFA_WHOLE, PLAN_NFA_WARP, PLAN_NFA_LANES, PLAN_DFA = 0, 1, 2, 3
 PLAN_HEADER_WORDS = 64
 (PLAN_STATUS, PLAN_LANE_CHUNKS, PLAN_CHUNKS, PLAN_LANE_FIRST, PLAN_LANE_TASKS,
  PLAN_PERSIST_TASKS, PLAN_FIXUP_TASKS, PLAN_LANE_BYTES, PLAN_WARP_BYTES, PLAN_OVERFLOW,
- PLAN_WHOLE, PLAN_DFA_INPUTS) = range(12)
+ PLAN_WHOLE, PLAN_DFA_INPUTS, PLAN_DFA_CHUNKS, PLAN_DFA_FIXUPS) = range(14)
 PLAN_SLICES = 16
 
-TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES, TASK_DFA_GROUP = 0, 1, 2, 3, 4
+(TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES, TASK_DFA_GROUP, TASK_DFA_CHUNK,
+ TASK_DFA_FIXUP) = range(7)
 LANE_CAPACITY = 4  # members a lane holds (kLaneSlots)
 CHUNK_RECORD_BYTES = 256
 STATIC_SCRATCH_BYTES = 32 << 20  # GBFSM_STATIC_SCRATCH_BYTES
@@ -216,9 +221,11 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_probe_copy": (ctypes.c_int, [_vp, _vp, _sz, _i32, _vp]),
     "gbfsm_pageable_access": (_i32, []),
     "gbfsm_gather_inputs": (ctypes.c_int, [_vp, _vp, _i32, _vp, _vp]),
+    "gbfsm_dfa_chunks_run": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp,
+                                            _P(ChunkIO), _i32, _vp, _vp, _vp, _vp, _vp]),
 }
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 _lib: ctypes.CDLL | None = None
 

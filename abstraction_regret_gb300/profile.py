@@ -1,0 +1,110 @@
+"""One small step of a named workload, for a profiler to capture.
+
+    python -m abstraction_regret_gb300.profile CASE [--steps N]
+
+Each case builds its batch, checks the verdicts of its first step against the oracle
+(the process exits non-zero on a difference), then runs ``--steps`` more steps and
+exits. Sizes are chosen so that a capture of every launch ends in seconds while the
+inputs stay larger than L2 where the case's kernel streams them:
+
+* ``c1-live``        the engine on c1 (1024-state NFA, 64 x 4 KiB random walks);
+* ``c1-plain``       the plain warp-per-input launch (``nfa_warp_kernel``) on c1;
+* ``c2-sustained``   the DFA cluster walk on c2-sustained (4096 x 64 KiB);
+* ``c4-sustained``   the engine on c4-sustained (64 NFAs, 1024 inputs; lanes and
+                     persistent launches);
+* ``dfa-long``       chunked DFA walks (``dfa_chunks_kernel``): 8 inputs of 2 MiB on
+                     the c2 DFA (4096 states, no accepting state).
+"""
+
+from __future__ import annotations
+
+import argparse
+import sys
+
+import numpy as np
+
+
+def _check(name, got, want) -> None:
+    for g, w, what in zip(got, want, ("flags", "lens", "examined")):
+        if g is not None and not np.array_equal(np.asarray(g), np.asarray(w)):
+            raise SystemExit(f"{name}: {what} differ from the oracle")
+
+
+def run(case: str, steps: int) -> None:
+    import torch
+
+    from oracle import oracle as O
+
+    from . import workloads as W
+    from .engine import GraphRunner, PersistentEngine
+    from .executors import CudaDFAExecutor, CudaNFAExecutor
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if case in ("c1-live", "c4-sustained", "dfa-long"):
+        if case == "c1-live":
+            b = W.c1("live")
+        elif case == "c4-sustained":
+            b = W.c4("sustained")
+        else:
+            b = W.c2("sustained")
+            n, length = 8, 2 << 20
+            b = W.Batch("dfa-long", b.automata, np.zeros(n, np.int64),
+                        W.uniform_bytes([1, 4], n * length),
+                        W.offsets_of(np.full(n, length, dtype=np.int64)), {})
+        r = GraphRunner(PersistentEngine(b.automata, dev), b.aut_ids, b.data, b.offsets,
+                        with_examined=True)
+        with torch.cuda.stream(r.stream):
+            r.replay()
+        r.stream.synchronize()
+        got = r.verdicts()
+        want = [np.zeros(b.n_inputs, np.int64) for _ in range(3)]
+        for k, a in enumerate(b.automata):
+            sel = np.flatnonzero(b.aut_ids == k)
+            if sel.size == 0:
+                continue
+            sub = b.subset(sel)
+            res = O.dfa_batch(a, sub.data, sub.offsets) if case == "dfa-long" else \
+                O.nfa_batch(a, sub.data, sub.offsets)[:3]
+            for w, v in zip(want, res):
+                w[sel] = v
+        _check(case, got, want)
+        with torch.cuda.stream(r.stream):
+            for _ in range(steps):
+                r.kernel_only(r.stream)
+        r.stream.synchronize()
+        return
+    if case == "c1-plain":
+        b = W.c1("live")
+        ex = CudaNFAExecutor(b.automata[0], "auto", dev)
+        want = O.nfa_batch(b.automata[0], b.data, b.offsets)[:2]
+    elif case == "c2-sustained":
+        b = W.c2("sustained")
+        ex = CudaDFAExecutor(b.automata[0], device=dev)
+        want = O.dfa_batch(b.automata[0], b.data, b.offsets)[:2]
+    else:
+        raise SystemExit(f"unknown case {case!r}")
+    stream = torch.cuda.current_stream(dev)
+    d = torch.from_numpy(b.data).to(dev)
+    off = torch.from_numpy(b.offsets).to(dev)
+    out = torch.zeros((2, b.n_inputs), dtype=torch.int32, device=dev)
+    ex.launch(d, off, b.n_inputs, out[0], out[1], None, stream)
+    stream.synchronize()
+    _check(case, (out[0].cpu().numpy(), out[1].cpu().numpy()), want)
+    for _ in range(steps):
+        ex.launch(d, off, b.n_inputs, out[0], out[1], None, stream)
+    stream.synchronize()
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("case", choices=["c1-live", "c1-plain", "c2-sustained", "c4-sustained",
+                                     "dfa-long"])
+    ap.add_argument("--steps", type=int, default=2)
+    args = ap.parse_args(argv)
+    run(args.case, args.steps)
+    print(f"{args.case}: verdicts equal to the oracle; {args.steps} more steps run")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

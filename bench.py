@@ -65,7 +65,7 @@ def parse_args(argv=None):
                     choices=["c3-sustained", "c3-live", "c3-literal"])
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline measurement (used for profiling)")
-    ap.add_argument("--extras", default="plain,run_batch,refgpu,c1,dfa,c4,serving",
+    ap.add_argument("--extras", default="plain,run_batch,refgpu,c1,dfa,dfa_chunks,c4,serving",
                     help="comma-separated extra sections after the headline")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the c5 serving trace (0: skip the serving section)")
@@ -194,6 +194,28 @@ def replica_throughput(offered_bytes: int, ms: float, world: int) -> float:
     return offered_bytes * world / (ms * 1e-3) / 1e9
 
 
+def step_stats(samples, total_bytes: int, iters: int = 2000, seed: int = 0) -> dict:
+    """Median step time with a percentile-bootstrap 95 % interval of the median
+    (``iters`` resamples of the steps with replacement, seeded so a rerun gives the same
+    interval), and the throughput at the median. Step times are skewed by the odd slow
+    step, so the median and its interval describe them better than a mean and a standard
+    deviation."""
+    a = np.asarray(samples, dtype=np.float64)
+    if a.size == 0:
+        return {"n": 0}
+    med = float(np.median(a))
+    if a.size > 1:
+        draws = np.random.default_rng(seed).integers(0, a.size, size=(iters, a.size))
+        meds = np.median(a[draws], axis=1)
+        lo, hi = float(np.percentile(meds, 2.5)), float(np.percentile(meds, 97.5))
+    else:
+        lo = hi = med
+    return {"median_ms": med, "ci95_ms": [lo, hi], "n": int(a.size),
+            "median_GBps": total_bytes / (med * 1e-3) / 1e9,
+            "method": f"median of {a.size} step times, percentile bootstrap CI95 of the "
+                      f"median ({iters} resamples, seed {seed})"}
+
+
 def time_launches(fn, stream, steps: int, warmup: int):
     """Mean ms per call of ``fn`` over ``steps`` calls (CUDA events on ``stream``)."""
     import torch
@@ -209,6 +231,76 @@ def time_launches(fn, stream, steps: int, warmup: int):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) / steps
+
+
+def cpu_port(one_pass, offered: int, what: str, budget_s: float = 5.0) -> dict:
+    """The oracle port on this host's cores for one extra configuration: whole passes
+    (``one_pass()`` runs the batch once, inputs spread over every thread) until
+    ``budget_s`` of wall time has gone; at least one pass. Offered bytes per second, the
+    unit of the extras."""
+    threads = os.cpu_count() or 1
+    passes = 0
+    t0 = time.perf_counter()
+    while True:
+        one_pass(threads)
+        passes += 1
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            break
+    return {"value": offered * passes / dt / 1e9, "unit": "GB/s", "cores": threads,
+            "kind": "port", "sample": f"{passes} whole passes over {what} in {dt:.1f} s"}
+
+
+def nfa_roofline(counts: dict, ms: float, onchip: dict | None) -> dict:
+    """Roofline of an NFA engine step from the oracle's counts (same rule as the
+    headline: per examined symbol 1 input byte, 8 bytes per active state, 8 per scanned
+    edge, 12 bytes of verdicts per input) against the L2 read bandwidth, with the latency
+    bound of its chains (lane chunks or whole inputs: one dependent L2 load per byte)."""
+    algo = counts["examined"] + 8 * counts["states"] + 8 * counts["edges"] + 12 * counts["n"]
+    achieved = algo / (ms * 1e-3) / 1e9
+    l2 = onchip.get("l2_read_GBps") if onchip else None
+    lat = onchip.get("l2_latency_ns") if onchip else None
+    sym = counts["examined"] / (ms * 1e-3) / 1e9
+    bound_sym = counts["chains"] / lat if lat and counts["chains"] else None
+    return {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
+            "frac": achieved / l2 if l2 else None, "algorithmic_bytes": int(algo),
+            "latency": {"chains": counts["chains"], "l2_latency_ns": lat,
+                        "bound_Gsymbols_per_s": bound_sym, "achieved_Gsymbols_per_s": sym,
+                        "frac": sym / bound_sym if bound_sym else None},
+            "peak_source": "measured in this run: L2 streaming read (gbfsm_probe_l2_read)"}
+
+
+def dfa_roofline(examined: int, chains: int, ms: float, onchip: dict | None,
+                 hbm: float) -> dict:
+    """Roofline of a DFA walk: every examined symbol is one dependent lookup of a 2-byte
+    table entry held on chip, so ``chains`` walks run at most chains / L2 latency symbols
+    per second; the input stream (1 byte per symbol) against HBM beside it."""
+    lat = onchip.get("l2_latency_ns") if onchip else None
+    sym = examined / (ms * 1e-3) / 1e9
+    bound = chains / lat if lat else None
+    return {"bound": "latency", "achieved": sym, "peak": bound, "unit": "Gsymbols/s",
+            "frac": sym / bound if bound else None, "chains": chains, "l2_latency_ns": lat,
+            "algorithmic_bytes": 3 * int(examined),
+            "input_stream": {"achieved": sym, "peak": hbm, "unit": "GB/s",
+                             "frac": sym / hbm},
+            "peak_source": "chains / L2 dependent-load latency measured in this run "
+                           "(gbfsm_probe_chase)"}
+
+
+def attach_rooflines(extras: dict, onchip: dict | None, hbm: float) -> None:
+    """Give the c1, c2 and c4 extras their roofline entries once the on-chip peaks have
+    been measured (the counts were stored by their sections)."""
+    for key in ("c1_plain_nfa", "c4_multi_automaton"):
+        for v in extras.get(key, {}).values():
+            c = v.pop("_counts", None)
+            if isinstance(v, dict) and c:
+                v["roofline"] = nfa_roofline(c, v["engine_ms"] if "engine_ms" in v else v["ms"],
+                                             onchip)
+    for key in ("dfa_c2_literal", "dfa_c2_sustained"):
+        v = extras.get(key)
+        if v and "_counts" in v:
+            c = v.pop("_counts")
+            v["roofline"].update(dfa_roofline(c["examined"], c["chains"], v["ms"], onchip, hbm))
 
 
 def cpu_reference(batch, budget_s: float = 15.0, threads: int | None = None):
@@ -329,16 +421,18 @@ def main(argv=None) -> int:
     clk = ClockSampler(local).__enter__()
     barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    # an event between consecutive steps gives per-step times for the median and its
+    # interval; the mean over the K steps (first to last event) is the headline
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with torch.cuda.stream(stream):
-        e0.record(stream)
+        marks[0].record(stream)
         launches = 0
-        for _ in range(args.steps):
+        for k in range(args.steps):
             launches += runner.kernel_only(stream, phases=phases)
-        e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+            marks[k + 1].record(stream)
+    marks[-1].synchronize()
+    ms = marks[0].elapsed_time(marks[-1]) / args.steps
+    step_samples = [marks[k].elapsed_time(marks[k + 1]) for k in range(args.steps)]
     torch.cuda.synchronize()
     barrier()
     ms = max_over_ranks(ms, dev, world)
@@ -419,6 +513,8 @@ def main(argv=None) -> int:
 
             of, ol, oe = O.dfa_batch(b2.automata[0], b2.data, b2.offsets)
             assert np.array_equal(f2, of) and np.array_equal(l2, ol), f"DFA c2-{variant} parity"
+            cpu2 = cpu_port(lambda t, b2=b2: O.dfa_batch(b2.automata[0], b2.data, b2.offsets, t),
+                            b2.total_bytes, f"c2-{variant} (4096 x 64 KiB)")
             examined_gbps = int(oe.sum()) / (d_ms * 1e-3) / 1e9
             hbm_peak = float(json.loads((REPO / "MEASURED_PEAKS.json").read_text())
                              .get("hbm_gbs", 6800.0)) \
@@ -434,7 +530,9 @@ def main(argv=None) -> int:
                              "hbm_frac_input_stream": examined_gbps / hbm_peak,
                              "chains": int(b2.n_inputs),
                              "ns_per_lookup_longest_chain": d_ms * 1e6 / max(1, longest)
-                             if variant == "sustained" else None}}
+                             if variant == "sustained" else None},
+                "cpu_baseline": cpu2,
+                "_counts": {"examined": int(oe.sum()), "chains": int(b2.n_inputs)}}
             del r2, ex2, b2
     if "run_batch" in sections and rank == 0:
         extras["run_batch_default"] = run_batch_section(batch, flags, lens, steps=3)
@@ -444,6 +542,8 @@ def main(argv=None) -> int:
         extras["c1_plain_nfa"] = c1_section(dev, max(2, args.steps // 2))
     if "c4" in sections and rank == 0:
         extras["c4_multi_automaton"] = c4_section(dev, max(2, args.steps // 2))
+    if "dfa_chunks" in sections and rank == 0:
+        extras["dfa_chunks"] = dfa_chunks_section(dev, max(2, args.steps // 4))
     if "serving" in sections and rank == 0 and args.serve_requests > 0:
         extras["serving"] = serving_section(dev, args.serve_requests, args.slo_ms)
 
@@ -453,6 +553,9 @@ def main(argv=None) -> int:
         from abstraction_regret_gb300 import peaks as P
 
         onchip = P.measure(dev)
+        attach_rooflines(extras, onchip, float(json.loads(
+            (REPO / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0))
+            if (REPO / "MEASURED_PEAKS.json").exists() else 6800.0)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     peaks = {}
@@ -534,6 +637,7 @@ def main(argv=None) -> int:
                                         f"of {info['chunks']} chunks), overlap-linked "
                                         "parallel fix-up"},
                 "phases_ms": phase_ms,
+                "step_stats": step_stats(step_samples, offered),
                 "e2e": e2e, "e2e_other_ingest": e2e_other, "gpu_launches": launches,
                 "oracle_gate": gate,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
@@ -675,7 +779,7 @@ def c1_section(dev, steps: int) -> dict:
     for variant in ("live", "sustained"):
         b = W.c1(variant)
         nfa = b.automata[0]
-        of, ol, oe, _ = O.nfa_batch(nfa, b.data, b.offsets)
+        of, ol, oe, _, work, visits = O.nfa_batch(nfa, b.data, b.offsets, with_work=True)
         r = GraphRunner(PersistentEngine([nfa], dev), b.aut_ids, b.data, b.offsets,
                         with_examined=True)
         with torch.cuda.stream(r.stream):
@@ -694,10 +798,17 @@ def c1_section(dev, steps: int) -> dict:
                                      r.stream, steps, 3)
         if not np.array_equal(d_out[0].cpu().numpy(), of):
             raise SystemExit(f"c1-{variant}: plain launch differs from the oracle")
+        info = r.plan_info()
         out[variant] = {"engine_GBps": b.total_bytes / (ms * 1e-3) / 1e9, "engine_ms": ms,
                         "plain_GBps": b.total_bytes / (plain_ms * 1e-3) / 1e9,
                         "plain_ms": plain_ms, "offered_bytes": int(b.total_bytes),
-                        "checked": int(f.size)}
+                        "checked": int(f.size),
+                        "cpu_baseline": cpu_port(
+                            lambda t: O.nfa_batch(nfa, b.data, b.offsets, t),
+                            b.total_bytes, f"c1-{variant} (64 x 4 KiB)"),
+                        "_counts": {"examined": int(oe.sum()), "states": int(visits.sum()),
+                                    "edges": int(work.sum()), "n": int(b.n_inputs),
+                                    "chains": int(info["lane_chunks"] or b.n_inputs)}}
         del r, plain
     return out
 
@@ -722,10 +833,16 @@ def c4_section(dev, steps: int) -> dict:
             r.replay()
         r.stream.synchronize()
         f, l, ex = r.verdicts()
+        counts = {"examined": 0, "states": 0, "edges": 0, "n": int(b.n_inputs)}
+        subsets = []
         for k, a in enumerate(b.automata):
             sel = np.flatnonzero(b.aut_ids == k)
             sub = b.subset(sel)
-            of, ol, oe, _ = O.nfa_batch(a, sub.data, sub.offsets)
+            subsets.append((a, sub))
+            of, ol, oe, _, work, visits = O.nfa_batch(a, sub.data, sub.offsets, with_work=True)
+            counts["examined"] += int(oe.sum())
+            counts["states"] += int(visits.sum())
+            counts["edges"] += int(work.sum())
             if not (np.array_equal(f[sel], of) and np.array_equal(l[sel], ol)
                     and np.array_equal(ex[sel], oe)):
                 raise SystemExit(f"c4-{variant}: automaton {k} differs from the oracle")
@@ -747,12 +864,78 @@ def c4_section(dev, steps: int) -> dict:
 
         with torch.cuda.stream(r.stream):
             plain_ms = time_launches(plain_all, r.stream, 1, 1)
+        info = r.plan_info()
+        counts["chains"] = int(info["lane_chunks"] + info["persistent_tasks"])
+
+        def cpu_pass(t, subsets=subsets):
+            for a_, sub_ in subsets:
+                O.nfa_batch(a_, sub_.data, sub_.offsets, t)
+
         out[variant] = {"offered_GBps": b.total_bytes / (ms * 1e-3) / 1e9,
                         "examined_GBps": int(ex.sum()) / (ms * 1e-3) / 1e9, "ms": ms,
                         "plain_per_automaton_ms": plain_ms,
                         "speedup_vs_plain_per_automaton": plain_ms / ms,
-                        "offered_bytes": int(b.total_bytes), "checked": int(f.size)}
+                        "offered_bytes": int(b.total_bytes), "checked": int(f.size),
+                        "cpu_baseline": cpu_port(cpu_pass, b.total_bytes,
+                                                 f"c4-{variant} (64 NFAs x 16 inputs)"),
+                        "_counts": counts}
         del r, eng, plains
+    return out
+
+
+def dfa_chunks_section(dev, steps: int) -> dict:
+    """Chunked DFA walks (DFA_CHUNK / DFA_FIXUP tasks) against whole-input walks (one lane
+    per input) in one engine step, on the c2 DFA (4096 states, no accepting state):
+    64 inputs of 4 MiB (chunks of the engine's own length), and c2-sustained itself (4096
+    inputs of 64 KiB, which the engine runs whole) with 16 KiB chunks forced. Verdicts
+    and examined counts bit-exact against the oracle first; device time per step
+    (planning included)."""
+    import torch
+
+    from abstraction_regret_gb300 import engine as E
+    from abstraction_regret_gb300 import workloads as W
+    from abstraction_regret_gb300.engine import GraphRunner, PersistentEngine
+    from oracle import oracle as O
+
+    c2 = W.c2("sustained")
+    dfa = c2.automata[0]
+    long_n, long_len = 64, 4 << 20
+    cases = {
+        "long_4MiB": (W.offsets_of(np.full(long_n, long_len, dtype=np.int64)),
+                      W.uniform_bytes([1, 3], long_n * long_len), None),
+        "c2_sustained": (c2.offsets, c2.data, 16 << 10),
+    }
+    out = {}
+    for name, (offsets, data, forced) in cases.items():
+        of, ol, oe = O.dfa_batch(dfa, data, offsets)
+        row = {"inputs": int(len(offsets) - 1), "bytes": int(offsets[-1])}
+        for mode, chunk in (("chunked", forced), ("whole", 0)):
+            eng = PersistentEngine([dfa], dev, dfa_chunk_bytes=chunk)
+            r = GraphRunner(eng, np.zeros(len(offsets) - 1, np.int64), data, offsets,
+                            with_examined=True)
+            with torch.cuda.stream(r.stream):
+                r.replay()
+            r.stream.synchronize()
+            f, l, ex = r.verdicts()
+            if not (np.array_equal(f, of) and np.array_equal(l, ol) and np.array_equal(ex, oe)):
+                raise SystemExit(f"DFA chunks {name}/{mode}: verdicts differ from the oracle")
+            info = r.plan_info()
+            with torch.cuda.stream(r.stream):
+                ms = time_launches(lambda: r.kernel_only(r.stream), r.stream,
+                                   steps if mode == "chunked" else 1, 1)
+            phases: dict = {}
+            with torch.cuda.stream(r.stream):
+                r.kernel_only(r.stream, phases=phases)
+            r.stream.synchronize()
+            row[mode] = {"ms": ms, "GBps": int(offsets[-1]) / (ms * 1e-3) / 1e9,
+                         "dfa_chunks": info.get("dfa_chunks", 0),
+                         "chunk_bytes": int(eng.dfa_chunk[0]),
+                         "phases_ms": {k: ev[0].elapsed_time(ev[1]) for k, ev in phases.items()
+                                       if len(ev) >= 2}}
+            del r, eng
+        row["speedup"] = row["whole"]["ms"] / row["chunked"]["ms"]
+        row["overlap_cap_bytes"] = E.dfa_overlap_bytes(dfa.num_states)
+        out[name] = row
     return out
 
 

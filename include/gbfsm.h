@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define GBFSM_ABI_VERSION 2
+#define GBFSM_ABI_VERSION 3
 #define GBFSM_ANY_SYMBOL 256 /* src/gpufsm/core/nfa.py:16 */
 #define GBFSM_WORD_BITS 64   /* src/gpufsm/core/packing.py:21 */
 
@@ -256,7 +256,8 @@ typedef struct gbfsm_automaton {
     int32_t kind;          /* 0 = NFA, 1 = DFA */
     int32_t technique;     /* NFA: GBFSM_TECH_WARP or GBFSM_TECH_COMPACT */
     int32_t list_capacity; /* NFA compact list capacity (<= the launch's capacity) */
-    int32_t reserved;
+    int32_t dfa_overlap;   /* DFA: bytes a DFA_CHUNK task's exact walk continues past its
+                              chunk's end (0 = none; every chunk then links by a walk) */
     gbfsm_nfa_dev nfa;     /* valid when kind == 0 */
     gbfsm_dfa_dev dfa;     /* valid when kind == 1 */
 } gbfsm_automaton;
@@ -287,6 +288,13 @@ typedef struct gbfsm_task {
 #define GBFSM_TASK_DFA_GROUP 4 /* inputs input_ids[first .. first + count), count <= 32, one
                                   DFA walk per lane, each on its input's own DFA
                                   (gbfsm_chunk_io.aut_ids); automaton is -1 */
+#define GBFSM_TASK_DFA_CHUNK 5 /* chunk `first` (count 1) of a long input of DFA `automaton`,
+                                  walked by a warp from the set of all states until it
+                                  collapses to one; its record goes to the chunk records
+                                  (gbfsm_dfa_chunks_run) */
+#define GBFSM_TASK_DFA_FIXUP 6 /* input whose DFA chunks are chunks[first .. first + count):
+                                  its exact verdict from their records, gaps walked
+                                  serially (gbfsm_dfa_chunks_run) */
 
 /* A piece of an NFA input: bytes data[begin .. end) of input `input`; `index` counts the
  * input's chunks from 0. Chunks after the first must start at least 2 bytes into the
@@ -406,14 +414,16 @@ gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_autom
                                   (the automaton needs first_row / first_edges) */
 #define GBFSM_PLAN_NFA_LANES 2 /* NFA: every input cut into lane chunks (the automaton
                                   needs the lane tables) */
-#define GBFSM_PLAN_DFA 3       /* DFA inputs, 32 per task, one walk per lane */
+#define GBFSM_PLAN_DFA 3       /* DFA inputs, 32 per task, one walk per lane; inputs of at
+                                  least twice the DFA's aut_dfa_chunk bytes are cut into
+                                  DFA chunks instead */
 
 /* Words of the plan header (int32, device). */
 #define GBFSM_PLAN_HEADER_WORDS 64
 #define GBFSM_PLAN_STATUS 0        /* 0 ok; 1 a capacity was too small; 2 an automaton id
                                       out of range. Not 0: every count below is 0. */
 #define GBFSM_PLAN_LANE_CHUNKS 1   /* chunks run one per lane: chunks[0 .. this) */
-#define GBFSM_PLAN_CHUNKS 2        /* all chunks (lane chunks, then warp chunks) */
+#define GBFSM_PLAN_CHUNKS 2        /* all chunks (lane chunks, warp chunks, DFA chunks) */
 #define GBFSM_PLAN_LANE_FIRST 3    /* always 0: {LANE_FIRST, LANE_TASKS} is the range of
                                       every LANES task for gbfsm_lanes_run_range */
 #define GBFSM_PLAN_LANE_TASKS 4
@@ -424,6 +434,9 @@ gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_autom
 #define GBFSM_PLAN_OVERFLOW 9      /* zeroed: the overflow_count of the lane launch */
 #define GBFSM_PLAN_WHOLE 10        /* whole NFA inputs: input_ids[0 .. this) */
 #define GBFSM_PLAN_DFA_INPUTS 11   /* DFA inputs: input_ids[WHOLE .. WHOLE + this) */
+#define GBFSM_PLAN_DFA_CHUNKS 12   /* task_count of the DFA chunk launch (chunks of long DFA
+                                      inputs, after the lane and warp chunks) */
+#define GBFSM_PLAN_DFA_FIXUPS 13   /* task_count of the DFA fix-up launch */
 #define GBFSM_PLAN_SLICES 16       /* {first, count} LANES task range of slice k at
                                       16 + 2k, for gbfsm_lanes_run_range */
 #define GBFSM_PLAN_MAX_SLICES 16
@@ -436,6 +449,8 @@ typedef struct gbfsm_batch_plan_args {
                                  offsets[i + 1] */
     const int32_t *aut_ids;   /* device [n_inputs] or NULL (all automaton 0) */
     const int32_t *aut_class; /* device [n_automata]: GBFSM_PLAN_* */
+    const int32_t *aut_dfa_chunk; /* device [n_automata] or NULL: DFA chunk bytes (0 = run
+                                     the DFA's inputs whole) */
     int32_t lane_warps;       /* resident warps of the lane launch (SMs x
                                  gbfsm_lanes_warps_per_sm) */
     int32_t persist_warps;    /* resident warps of the persistent launch */
@@ -450,10 +465,16 @@ typedef struct gbfsm_batch_plan_args {
     int32_t cap_lane_tasks;
     int32_t cap_persist_tasks;
     int32_t cap_fixup_tasks;
+    int32_t cap_dfa_chunk_tasks;
+    int32_t cap_dfa_fixup_tasks;
     gbfsm_chunk *chunks;          /* device [cap_chunks] */
     gbfsm_task *tasks_lanes;      /* device [cap_lane_tasks] */
     gbfsm_task *tasks_persist;    /* device [cap_persist_tasks] */
     gbfsm_task *tasks_fixup;      /* device [cap_fixup_tasks] */
+    gbfsm_task *tasks_dfa_chunk;  /* device [cap_dfa_chunk_tasks] (needed with aut_dfa_chunk) */
+    gbfsm_task *tasks_dfa_fixup;  /* device [cap_dfa_fixup_tasks] (needed with aut_dfa_chunk) */
+    int32_t *dfa_latch;           /* device [n_inputs] or NULL: set to INT32_MAX for every
+                                     chunked DFA input (the latch of gbfsm_dfa_chunks_run) */
     int32_t *input_ids;           /* device [n_inputs] */
     int32_t *header;              /* device [GBFSM_PLAN_HEADER_WORDS] */
     void *scratch;                /* device, gbfsm_batch_plan_scratch_bytes(n_inputs) */
@@ -465,6 +486,29 @@ size_t gbfsm_batch_plan_scratch_bytes(int32_t n_inputs);
 /* Enqueue the planning launches on `stream`. Validates the arguments on the host;
  * device-side failures (capacity, automaton ids) are reported in the header's status. */
 gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *args, void *stream);
+
+/* Run DFA_CHUNK or DFA_FIXUP tasks (others are skipped): min(*task_count, max_tasks)
+ * tasks of `tasks` when task_count is non-NULL, else max_tasks. A step runs the DFA_CHUNK
+ * tasks of a batch first, then its DFA_FIXUP tasks in a later launch on the same stream;
+ * both read chunk_io->chunks and share chunk_io->records (the first 32 bytes of each
+ * chunk's record). max_states: the most states of any DFA the tasks name (1..32768; each
+ * warp holds two bitmaps of that many bits in shared memory). A DFA_FIXUP task writes its
+ * input's flags / lens (and examined) entries. Input i is data[offsets[i] .. ends[i]) when
+ * `ends` is non-NULL, else data[offsets[i] .. offsets[i + 1]). latch (device [n_inputs] or
+ * NULL) lets an input's chunks stop early: a chunk that finds an accept certain to be in
+ * the input's true walk lowers latch[input] to its index (atomicMin), and a chunk of a
+ * higher index stops walking once it sees that -- the verdict lies before it. Its entries
+ * must hold INT32_MAX for the chunked inputs when the DFA_CHUNK launch starts
+ * (gbfsm_batch_plan writes them when given dfa_latch). No counterpart in the
+ * reference, whose DFA kernel walks each input serially with one thread
+ * (src/gpufsm/backends/cuda/native/dfa.cu). */
+gbfsm_status gbfsm_dfa_chunks_run(const gbfsm_automaton *table, int32_t n_automata,
+                                  const gbfsm_task *tasks, int32_t max_tasks,
+                                  const int32_t *task_count, const uint8_t *data,
+                                  const int64_t *offsets, const int64_t *ends,
+                                  const gbfsm_chunk_io *chunk_io, int32_t max_states,
+                                  int32_t *flags, int32_t *lens, int32_t *examined,
+                                  int32_t *latch, void *stream);
 
 /* Occupancy query for persistent launches: CTAs of `plan` resident per SM. */
 int32_t gbfsm_persistent_ctas_per_sm(int32_t max_words, const gbfsm_plan *plan);

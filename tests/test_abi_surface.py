@@ -60,6 +60,11 @@ def test_python_binding_covers_the_header(lib):
     assert lib.gbfsm_abi_version() == native.ABI_VERSION
 
 
+PLAN_FIELDS = ("aut_dfa_chunk", "lane_warps", "slice_first", "cap_chunks",
+               "cap_dfa_chunk_tasks", "cap_dfa_fixup_tasks", "chunks", "tasks_dfa_chunk",
+               "tasks_dfa_fixup", "dfa_latch", "input_ids", "scratch")
+
+
 def test_struct_layouts_match_the_header(tmp_path):
     """Compile a probe against include/gbfsm.h and compare every struct with ctypes."""
     pairs = {"gbfsm_edge": native.Edge, "gbfsm_nfa_dev": native.NfaDev,
@@ -75,14 +80,16 @@ def test_struct_layouts_match_the_header(tmp_path):
     lines.append('  printf("static %u\\n", GBFSM_STATIC_SCRATCH_BYTES);')
     for name in ("STATUS", "LANE_CHUNKS", "CHUNKS", "LANE_FIRST", "LANE_TASKS",
                  "PERSIST_TASKS", "FIXUP_TASKS", "LANE_BYTES", "WARP_BYTES", "OVERFLOW",
-                 "WHOLE", "DFA_INPUTS", "SLICES", "MAX_SLICES", "HEADER_WORDS", "NFA_WHOLE",
+                 "WHOLE", "DFA_INPUTS", "DFA_CHUNKS", "DFA_FIXUPS", "SLICES", "MAX_SLICES", "HEADER_WORDS", "NFA_WHOLE",
                  "NFA_WARP", "NFA_LANES", "DFA"):
         lines.append(f'  printf("PLAN_{name} %d\\n", GBFSM_PLAN_{name});')
-    lines.append('  printf("TASK_DFA_GROUP %d\\n", GBFSM_TASK_DFA_GROUP);')
-    for field in ("slice_first", "cap_chunks", "chunks", "scratch"):
+    for name in ("DFA_GROUP", "DFA_CHUNK", "DFA_FIXUP"):
+        lines.append(f'  printf("TASK_{name} %d\\n", GBFSM_TASK_{name});')
+    for field in PLAN_FIELDS:
         lines.append(f'  printf("off_{field} %zu\\n", '
                      f'offsetof(gbfsm_batch_plan_args, {field}));')
     lines.append('  printf("off_aut_ids %zu\\n", offsetof(gbfsm_chunk_io, aut_ids));')
+    lines.append('  printf("off_dfa_overlap %zu\\n", offsetof(gbfsm_automaton, dfa_overlap));')
     lines.append("  return 0; }")
     src.write_text("\n".join(lines))
     exe = tmp_path / "probe"
@@ -97,9 +104,10 @@ def test_struct_layouts_match_the_header(tmp_path):
     for key, value in out.items():
         if key.startswith(("PLAN_", "TASK_")):
             assert int(value) == getattr(native, key), key
-    for field in ("slice_first", "cap_chunks", "chunks", "scratch"):
+    for field in PLAN_FIELDS:
         assert int(out[f"off_{field}"]) == getattr(native.BatchPlanArgs, field).offset, field
     assert int(out["off_aut_ids"]) == native.ChunkIO.aut_ids.offset
+    assert int(out["off_dfa_overlap"]) == native.Automaton.dfa_overlap.offset
 
 
 def test_invalid_arguments_return_status_codes(lib):
@@ -128,6 +136,23 @@ def test_invalid_arguments_return_status_codes(lib):
     st = lib.gbfsm_nfa_run_static(None, None, None, 4, ctypes.byref(plan), None, None, None,
                                   None)
     assert st == native.INVALID_ARG
+    # DFA chunk launches: argument checks come before any device work
+    assert lib.gbfsm_dfa_chunks_run(None, 0, None, 0, None, None, None, None, None, 1, None,
+                                    None, None, None, None) == native.OK
+    st = lib.gbfsm_dfa_chunks_run(p, 1, p, 4, None, p, p, None, None, 16, p, p, None, None,
+                                  None)
+    assert st == native.INVALID_ARG and "NULL" in native.last_error()
+    io.chunks, io.records, io.n_chunks = p, p, 4
+    st = lib.gbfsm_dfa_chunks_run(p, 1, p, 4, None, p, p, None, ctypes.byref(io), 40000, p, p,
+                                  None, None, None)
+    assert st == native.INVALID_ARG and "max_states" in native.last_error()
+    a = native.BatchPlanArgs()
+    a.n_inputs, a.n_automata, a.min_chunk, a.cap_chunks = 4, 1, 64, 8
+    for f in ("offsets", "aut_class", "chunks", "tasks_lanes", "tasks_persist", "tasks_fixup",
+              "input_ids", "header", "scratch", "aut_dfa_chunk"):
+        setattr(a, f, p)
+    st = lib.gbfsm_batch_plan(ctypes.byref(a), None)
+    assert st == native.INVALID_ARG and "aut_dfa_chunk" in native.last_error()
 
 
 def test_status_mapping_raises_the_reference_exception_types():
