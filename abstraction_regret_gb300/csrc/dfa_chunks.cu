@@ -49,15 +49,24 @@ __global__ void __launch_bounds__(kDfaChunkThreads) dfa_chunks_kernel(
         if (task.kind == GBFSM_TASK_DFA_CHUNK) {
             DfaChunkRecord *rec = dfa_record(records, task.first);
             // the next chunk of the input, when there is one, is the next table entry
-            const DfaChunkRecord *next =
-                task.first + 1 < n_chunks ? dfa_record(records, task.first + 1) : nullptr;
+            const DfaChunkRecord *next = nullptr;
+            int64_t e_next = ch.end - off;
+            if (task.first + 1 < n_chunks) {
+                const gbfsm_chunk nx = chunks[task.first + 1];
+                if (nx.input == ch.input && nx.index == ch.index + 1) {
+                    next = dfa_record(records, task.first + 1);
+                    e_next = nx.end - off;
+                }
+            }
             int32_t *lt = latch ? latch + ch.input : nullptr;
             if (d.entry_bytes == 2)
                 dfa_chunk<uint16_t>(d, T.dfa_overlap, data + off, len, ch.begin - off,
-                                    ch.end - off, ch.index, bm0, bm1, list, rec, next, lt);
+                                    ch.end - off, e_next, ch.index, bm0, bm1, list, rec, next,
+                                    lt);
             else
                 dfa_chunk<uint32_t>(d, T.dfa_overlap, data + off, len, ch.begin - off,
-                                    ch.end - off, ch.index, bm0, bm1, list, rec, next, lt);
+                                    ch.end - off, e_next, ch.index, bm0, bm1, list, rec, next,
+                                    lt);
         } else if (lane == 0) {
             const Verdict v =
                 d.entry_bytes == 2
@@ -73,6 +82,49 @@ __global__ void __launch_bounds__(kDfaChunkThreads) dfa_chunks_kernel(
     }
 }
 
+// Shared scratch of a CTA for DFAs of up to `words` x 32 states.
+size_t dfa_chunks_smem(uint32_t words) {
+    return (size_t)kDfaChunkWarps * (2u * words + 32u) * sizeof(uint32_t);
+}
+
+// Resident CTAs per SM for that scratch, asked once per (device, scratch size): later
+// launches and graph captures reuse the answer. Opts the kernel in to the shared memory
+// it needs above 48 KiB; -1 when that is more than the device has.
+int dfa_chunks_blocks_per_sm(uint32_t words, gbfsm_status &st) {
+    static std::mutex mu;
+    static std::map<std::pair<int, uint32_t>, int> occupancy;
+    st = GBFSM_OK;
+    const size_t smem = dfa_chunks_smem(words);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        st = GBFSM_CUDA_ERROR;
+        return 0;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(dev, words);
+    const auto it = occupancy.find(key);
+    if (it != occupancy.end()) return it->second;
+    if (smem > 48u * 1024u) {
+        if (smem + kSmemReserve > (size_t)smem_optin()) return -1;
+        if (cudaFuncSetAttribute(dfa_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            st = GBFSM_CUDA_ERROR;
+            return 0;
+        }
+    }
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, dfa_chunks_kernel,
+                                                      kDfaChunkThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        st = GBFSM_CUDA_ERROR;
+        return 0;
+    }
+    occupancy[key] = blocks;
+    return blocks;
+}
+
 }  // namespace
 
 gbfsm_status launch_dfa_chunks(const gbfsm_automaton *table, int32_t n_automata,
@@ -84,34 +136,13 @@ gbfsm_status launch_dfa_chunks(const gbfsm_automaton *table, int32_t n_automata,
                                int32_t *latch, cudaStream_t stream) {
     if (max_tasks <= 0) return GBFSM_OK;
     const uint32_t words = ((uint32_t)max_states + 31u) >> 5;
-    const size_t smem = (size_t)kDfaChunkWarps * (2u * words + 32u) * sizeof(uint32_t);
-    if (smem > 48u * 1024u) {
-        if (smem + kSmemReserve > (size_t)smem_optin())
-            return fail(GBFSM_UNSUPPORTED, "DFA chunk walks of %d states need %zu shared bytes",
-                        max_states, smem);
-        GBFSM_CUDA_TRY(cudaFuncSetAttribute(dfa_chunks_kernel,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-    }
-    // resident CTAs per SM, asked once per (device, scratch size): later launches and
-    // graph captures reuse the answer
-    static std::mutex mu;
-    static std::map<std::pair<int, uint32_t>, int> occupancy;
-    int dev = 0;
-    GBFSM_CUDA_TRY(cudaGetDevice(&dev));
-    int blocks = 0;
-    {
-        std::lock_guard<std::mutex> lock(mu);
-        const auto key = std::make_pair(dev, words);
-        const auto it = occupancy.find(key);
-        if (it != occupancy.end()) {
-            blocks = it->second;
-        } else {
-            GBFSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &blocks, dfa_chunks_kernel, kDfaChunkThreads, smem));
-            occupancy[key] = blocks;
-        }
-    }
+    const size_t smem = dfa_chunks_smem(words);
+    gbfsm_status st = GBFSM_OK;
+    const int blocks = dfa_chunks_blocks_per_sm(words, st);
+    if (st != GBFSM_OK) return fail(st, "dfa_chunks_kernel: occupancy query failed");
+    if (blocks < 0)
+        return fail(GBFSM_UNSUPPORTED, "DFA chunk walks of %d states need %zu shared bytes",
+                    max_states, smem);
     int grid = sm_count() * (blocks > 0 ? blocks : 1);
     const int needed = (max_tasks + kDfaChunkWarps - 1) / kDfaChunkWarps;
     if (grid > needed) grid = needed;
@@ -123,6 +154,14 @@ gbfsm_status launch_dfa_chunks(const gbfsm_automaton *table, int32_t n_automata,
 }
 
 }  // namespace gbfsm
+
+extern "C" int32_t gbfsm_dfa_chunks_warps_per_sm(int32_t max_states) {
+    using namespace gbfsm;
+    if (max_states < 1 || max_states > 32768) return 0;
+    gbfsm_status st = GBFSM_OK;
+    const int blocks = dfa_chunks_blocks_per_sm(((uint32_t)max_states + 31u) >> 5, st);
+    return st == GBFSM_OK && blocks > 0 ? blocks * kDfaChunkWarps : 0;
+}
 
 extern "C" gbfsm_status gbfsm_dfa_chunks_run(const gbfsm_automaton *table, int32_t n_automata,
                                              const gbfsm_task *tasks, int32_t max_tasks,

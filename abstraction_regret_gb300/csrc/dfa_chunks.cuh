@@ -13,10 +13,12 @@
 //
 // The overlap is as long as the next chunk needs: a chunk publishes its collapse position
 // in its record as soon as it has it, and the previous chunk's overlap walk, polling that
-// word, stops once it has passed it (or at once when the next chunk never collapsed or
-// stopped), and in any case after `overlap` bytes (the automaton's dfa_overlap). A stale
-// word (the next chunk's task not started yet) can only cut an overlap short; the fix-up
-// checks every link against the final records, so verdicts never depend on the timing.
+// word, stops once it has passed it (at once when the next chunk stopped early), and in
+// any case at the next chunk's end or after `overlap` bytes (the automaton's
+// dfa_overlap). When the next chunk never collapses, the overlap covers it whole and
+// records the true state at its end, so the fix-up need not walk it. A stale word (the
+// next chunk's task not started yet) can only cut an overlap short; the fix-up checks
+// every link against the final records, so verdicts never depend on the timing.
 //
 // Fix-up (one lane per input, serial over the input's chunks): the true state at each
 // chunk start is known from the previous chunk's record. Chunk k is linked when chunk
@@ -54,9 +56,11 @@ struct DfaChunkRecord {
     int32_t end_state;
     int32_t ov_len;   // bytes walked past the chunk end (exact when p >= 0)
     int32_t ov_acc;   // first accept in the overlap, -1: none
-    int32_t pad[3];
+    int32_t ov_state; // the state at the end of the overlap (when ov_acc < 0)
+    int32_t pad[2];
 };
-static_assert(sizeof(DfaChunkRecord) <= GBFSM_CHUNK_RECORD_BYTES, "DFA chunk record slot");
+static_assert(sizeof(DfaChunkRecord) == 32 && sizeof(DfaChunkRecord) <= GBFSM_CHUNK_RECORD_BYTES,
+              "DFA chunk record slot");
 
 __device__ __forceinline__ DfaChunkRecord *dfa_record(void *records, int32_t chunk) {
     return reinterpret_cast<DfaChunkRecord *>(static_cast<uint8_t *>(records) +
@@ -238,17 +242,18 @@ __device__ int64_t dfa_collapse(const Entry *T, uint32_t n, const uint8_t *base,
 
 // One lane: the overlap walk of a chunk ending at e, from its exact state s, into the next
 // chunk (record `next`, or NULL when e is the input's end): until the next chunk's
-// published collapse position has been passed, or it is known that the next chunk never
-// collapsed or stopped, or `cap` is reached. Returns the overlap's length; its first
-// accept goes to ov_acc (-1 when none), and `stopped` is set when a chunk below `index`
-// latched the input meanwhile.
+// published collapse position has been passed, or it is known that the next chunk
+// stopped, or `cap` (at most the next chunk's end) is reached. Returns the overlap's
+// length; its first accept goes to ov_acc (-1 when none), the state at its end to
+// `s_end`, and `stopped` is set when a chunk below `index` latched the input meanwhile.
 template <typename Entry>
 __device__ int64_t dfa_overlap_walk(const Entry *T, uint32_t s, const uint8_t *base,
                                     int64_t e, int64_t cap, const DfaChunkRecord *next,
                                     const int32_t *latch, int32_t index, int64_t &ov_acc,
-                                    bool &stopped) {
+                                    uint32_t &s_end, bool &stopped) {
     constexpr uint32_t ACC = EntryTraits<Entry>::kAccept;
     ov_acc = -1;
+    s_end = s;
     if (cap <= e || !next) return 0;
     ByteStream bs;
     bs.init(base + e, cap - e);
@@ -260,27 +265,30 @@ __device__ int64_t dfa_overlap_walk(const Entry *T, uint32_t s, const uint8_t *b
         }
         const int32_t np = __ldcv(&next->p);
         if (np >= 0) target = min(target, max((int64_t)np, q));
-        else if (np == -1 || np == -2) target = q;
+        else if (np == -2) target = q;  // -1 (never collapsed): on to the cap
         const int64_t q1 = min(target, q + (int64_t)kLatchPollBytes);
         for (; q < q1; ++q) {
             const uint32_t x = dfa_entry(T, s, bs.next());
             s = x & ~ACC;
             if (x & ACC) {
                 ov_acc = q + 1;
+                s_end = s;
                 return ov_acc - e;
             }
         }
     }
+    s_end = s;
     return q - e;
 }
 
 // A DFA_CHUNK task: chunk `index` of an input spanning positions [b, e) of `base` (the
 // input's first byte), `len` bytes in all; the record goes to rec (the next chunk's, when
-// e < len, is rec_next). latch: the input's latch word, or NULL.
+// e < len, is rec_next, and that chunk ends at e_next). latch: the input's latch word, or
+// NULL.
 template <typename Entry>
 __device__ void dfa_chunk(const gbfsm_dfa_dev &d, int32_t overlap, const uint8_t *base,
-                          int64_t len, int64_t b, int64_t e, int index, uint32_t *bm0,
-                          uint32_t *bm1, uint32_t *list, DfaChunkRecord *rec,
+                          int64_t len, int64_t b, int64_t e, int64_t e_next, int index,
+                          uint32_t *bm0, uint32_t *bm1, uint32_t *list, DfaChunkRecord *rec,
                           const DfaChunkRecord *rec_next, int32_t *latch) {
     const Entry *T = static_cast<const Entry *>(d.table);
     const uint32_t lane = lane_id();
@@ -299,13 +307,15 @@ __device__ void dfa_chunk(const gbfsm_dfa_dev &d, int32_t overlap, const uint8_t
     }
     if (lane == 0) {
         int64_t ov_len = 0, ov_acc = -1;
+        uint32_t ov_state = 0;
         bool stopped = false;
         if (p >= 0 && acc < 0) {
             s = dfa_span<Entry>(T, s, base, p, e, acc, latch, index, &stopped);
             if (acc < 0 && !stopped) {
-                const int64_t cap = min(e + (int64_t)(overlap > 0 ? overlap : 0), len);
+                const int64_t cap =
+                    min(min(e + (int64_t)(overlap > 0 ? overlap : 0), e_next), len);
                 ov_len = dfa_overlap_walk<Entry>(T, s, base, e, cap, e < len ? rec_next : nullptr,
-                                                 latch, index, ov_acc, stopped);
+                                                 latch, index, ov_acc, ov_state, stopped);
                 if (latch && ov_acc >= 0) atomicMin(latch, index + 1);
             }
         }
@@ -315,14 +325,9 @@ __device__ void dfa_chunk(const gbfsm_dfa_dev &d, int32_t overlap, const uint8_t
             acc = ov_acc = -1;
             ov_len = 0;
         }
-        DfaChunkRecord r;
-        r.p = (int32_t)p;
-        r.acc = (int32_t)acc;
-        r.end_state = (int32_t)s;
-        r.ov_len = (int32_t)ov_len;
-        r.ov_acc = (int32_t)ov_acc;
-        r.pad[0] = r.pad[1] = r.pad[2] = 0;
-        *rec = r;
+        int4 *w = reinterpret_cast<int4 *>(rec);
+        w[0] = make_int4((int32_t)p, (int32_t)acc, (int32_t)s, (int32_t)ov_len);
+        w[1] = make_int4((int32_t)ov_acc, (int32_t)ov_state, 0, 0);
     }
     __syncwarp();
 }
@@ -339,6 +344,7 @@ __device__ Verdict dfa_fixup(const gbfsm_dfa_dev &d, const uint8_t *base, int64_
     uint32_t s = (uint32_t)r0.end_state;
     bool prev_ok = true;  // the previous chunk's walk and overlap are exact
     int64_t prev_ov_len = r0.ov_len, prev_ov_acc = r0.ov_acc;
+    uint32_t prev_ov_state = (uint32_t)r0.ov_state;
     for (int32_t k = 1; k < count; ++k) {
         if (prev_ok && prev_ov_acc >= 0) return Verdict{1, (int32_t)prev_ov_acc, prev_ov_acc};
         const gbfsm_chunk ch = chunks[first + k];
@@ -355,9 +361,14 @@ __device__ Verdict dfa_fixup(const gbfsm_dfa_dev &d, const uint8_t *base, int64_
             prev_ok = true;
             prev_ov_len = r.ov_len;
             prev_ov_acc = r.ov_acc;
+            prev_ov_state = (uint32_t)r.ov_state;
         } else {
-            s = dfa_span<Entry>(T, s, base, b, e, acc);  // never collapsed: the whole chunk
-            if (acc >= 0) return Verdict{1, (int32_t)acc, acc};
+            if (prev_ok && prev_ov_len == e - b) {
+                s = prev_ov_state;  // never collapsed, but the previous overlap covered it
+            } else {
+                s = dfa_span<Entry>(T, s, base, b, e, acc);  // never collapsed: walk it
+                if (acc >= 0) return Verdict{1, (int32_t)acc, acc};
+            }
             prev_ok = false;
         }
     }

@@ -5,7 +5,10 @@
 // plan_scan_kernel (one CTA of 1024 threads):
 //   1. classify every input by its automaton's class (whole-input NFA, warp-chunked NFA,
 //      lane-chunked NFA, DFA) and sum the bytes of the lane and warp classes;
-//   2. choose the chunk sizes: lane chunks get the smallest multiple of 64 bytes (at
+//   2. choose the chunk sizes: DFA chunks of an input are max(its DFA's shortest chunk,
+//      B / dfa_warps) bytes (B: the bytes of the DFA inputs holding two chunks of their
+//      own minimum), so that a batch of few long inputs gets short chunks and a large
+//      one a single wave of them; lane chunks get the smallest multiple of 64 bytes (at
 //      least min_chunk) whose chunks fill at most one wave of the lane launch (32 chunks
 //      per resident warp) -- found by an exponential then binary search, each probe a
 //      block-wide sum; warp chunks get a power of two giving about four chunks per
@@ -187,16 +190,34 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
     __syncthreads();
 
     // 1. classes and the bytes of the chunked classes
-    int64_t lane_bytes = 0, warp_bytes = 0;
+    int64_t lane_bytes = 0, warp_bytes = 0, dfa_bytes = 0, dfa_long = 0;
     for (int32_t i = lo; i < hi; ++i) {
         const InputInfo r = input_info(a, i);
         s.cls[i] = r.cls;
         if (r.cls < 0) bad = 1;
         if (r.cls == GBFSM_PLAN_NFA_LANES) lane_bytes += r.len;
         if (r.cls == GBFSM_PLAN_NFA_WARP) warp_bytes += r.len;
+        if (r.cls == GBFSM_PLAN_DFA && a.aut_dfa_chunk) {
+            const int64_t m = a.aut_dfa_chunk[r.aut];
+            if (m > 0 && r.len >= 2 * m) {
+                dfa_bytes += r.len;
+                dfa_long += 1;
+            }
+        }
     }
     lane_bytes = block_sum(lane_bytes, red);
     warp_bytes = block_sum(warp_bytes, red);
+    dfa_bytes = block_sum(dfa_bytes, red);
+    dfa_long = block_sum(dfa_long, red);
+    // the batch's DFA chunk length (before each DFA's minimum): rounding each input up to
+    // whole chunks adds at most one chunk per input, so B / (warps - inputs) keeps the
+    // chunks within one wave
+    int64_t dfa_target = 0;
+    if (a.dfa_warps > 0 && dfa_bytes > 0) {
+        const int64_t w = a.dfa_warps > dfa_long ? a.dfa_warps - dfa_long : 1;
+        dfa_target = ((dfa_bytes + w - 1) / w + 63) / 64 * 64;
+        if (dfa_target > (int64_t)1 << 30) dfa_target = (int64_t)1 << 30;
+    }
 
     // 2. chunk sizes
     int64_t lane_base = a.min_chunk;
@@ -261,9 +282,10 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
         const int32_t c = s.cls[i];
         const int64_t len = input_len(a, i);
         int64_t cnt = 0;
-        const int64_t dfa_chunk = (c == GBFSM_PLAN_DFA && a.aut_dfa_chunk)
-                                      ? (int64_t)a.aut_dfa_chunk[a.aut_ids ? a.aut_ids[i] : 0]
-                                      : 0;
+        int64_t dfa_chunk = (c == GBFSM_PLAN_DFA && a.aut_dfa_chunk)
+                                ? (int64_t)a.aut_dfa_chunk[a.aut_ids ? a.aut_ids[i] : 0]
+                                : 0;
+        if (dfa_chunk > 0 && dfa_target > dfa_chunk) dfa_chunk = dfa_target;
         if (c == GBFSM_PLAN_DFA && dfa_chunk > 0 && len >= 2 * dfa_chunk) {
             // a long DFA input: cut into chunks walked in parallel (DFA_CHUNK tasks)
             cnt = chunks_of(len, dfa_chunk);
@@ -360,6 +382,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
             h[GBFSM_PLAN_DFA_INPUTS] = d;
             h[GBFSM_PLAN_DFA_CHUNKS] = over ? 0 : (int32_t)n_dfa_chunks;
             h[GBFSM_PLAN_DFA_FIXUPS] = over ? 0 : (int32_t)n_dfa_split;
+            h[GBFSM_PLAN_DFA_CHUNK_BYTES] = (int32_t)dfa_target;
             // lane task range of each slice: task t waits for the slice holding the input
             // of its last chunk, min(32 t + 31, n_lane - 1)
             const int ns = a.n_slices > 1 ? a.n_slices : 1;

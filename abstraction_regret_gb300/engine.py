@@ -55,23 +55,33 @@ LANE_PAIR_MEAN = 32.0
 # CTAs, 8 per SM: csrc/lanes.cu)
 LANE_WARPS_PER_SM = 32
 # DFA chunking (csrc/dfa_chunks.cu): the largest DFA whose inputs are chunked (2-byte
-# table entries), the shortest DFA chunk, and the chunk and overlap lengths per state
+# table entries), and the shortest DFA chunk: at least DFA_CHUNK_MIN bytes and
+# DFA_CHUNK_PER_STATE bytes per state. A random DFA's set of all states collapses after
+# about 2n bytes, with a tail of about e^(-t/n) beyond; at 8n a chunk rarely ends before
+# it collapses (at 2n about half do, and their fix-up turns serial). The planner
+# lengthens the chunks of a batch with many long DFA inputs to one wave of the chunk
+# launch.
 DFA_CHUNK_MAX_STATES = 32768
-DFA_CHUNK_MIN = 64 << 10
+DFA_CHUNK_MIN = 16 << 10
 DFA_CHUNK_FLOOR = 4096  # the shortest DFA chunk a caller may ask for
 DFA_CHUNK_PER_STATE = 8
-DFA_OVERLAP_PER_STATE = 12
+# the most a DFA chunk's exact walk continues into the next chunk, as a share of the
+# shortest chunk; 1 or more: no limit but the next chunk's end (the walk stops at that
+# chunk's collapse, or covers it whole when it never collapses)
+DFA_OVERLAP_CHUNKS = 1.0
 
 
 def dfa_chunk_length(num_states: int) -> int:
-    """Chunk length for the long inputs of a DFA of ``num_states`` states (a multiple of
-    64 bytes): its set of all states must usually collapse well inside one chunk."""
+    """Shortest chunk for the long inputs of a DFA of ``num_states`` states (a multiple of
+    64 bytes); an input is chunked when it holds two chunks."""
     return -(-max(DFA_CHUNK_MIN, DFA_CHUNK_PER_STATE * int(num_states)) // 64) * 64
 
 
-def dfa_overlap_bytes(num_states: int) -> int:
+def dfa_overlap_bytes(chunk_length: int) -> int:
     """Most bytes a DFA chunk's exact walk continues into the next chunk."""
-    return DFA_OVERLAP_PER_STATE * int(num_states)
+    if DFA_OVERLAP_CHUNKS >= 1.0:
+        return 1 << 30
+    return int(DFA_OVERLAP_CHUNKS * int(chunk_length))
 
 
 @dataclass
@@ -276,6 +286,7 @@ class DevicePlan:
         a.cap_dfa_fixup_tasks = self.cap_dfa_fixup
         a.lane_warps = eng.sm_count * eng.lane_warps_per_sm
         a.persist_warps = eng.resident_warps
+        a.dfa_warps = eng.dfa_warps
         a.min_chunk = MIN_CHUNK
         a.fixed_chunk = eng.fixed_chunk
         if self.slices:
@@ -462,9 +473,10 @@ class PersistentEngine:
                                                                      ctypes.byref(self.plan)))
             self.workspace = torch.zeros(self.ws_bytes, dtype=torch.uint8, device=self.device)
             # long DFA inputs are cut into chunks walked in parallel (DFA_CHUNK tasks): a
-            # chunk of an n-state DFA spans max(64 KiB, 8n) bytes, and its exact walk
-            # continues into the next chunk until it passes that chunk's collapse (about
-            # 2n bytes in for a random DFA), for at most 12n bytes
+            # chunk of an n-state DFA spans at least max(16 KiB, 8n) bytes, and its exact
+            # walk continues into the next chunk until it passes that chunk's collapse
+            # (about 2n bytes in for a random DFA), or over all of it when it never
+            # collapses
             dfa_chunk = [0] * len(self.automata)
             if chunk_bytes is not None and dfa_chunk_bytes != 0:
                 for i, (d, k) in enumerate(zip(self.dev, self.kinds)):
@@ -486,7 +498,7 @@ class PersistentEngine:
                 else:
                     table[i].kind = 1
                     table[i].dfa = d.desc
-                    table[i].dfa_overlap = dfa_overlap_bytes(d.num_states) if dfa_chunk[i] else 0
+                    table[i].dfa_overlap = dfa_overlap_bytes(dfa_chunk[i])
             raw = np.frombuffer(bytes(table), dtype=np.uint8).copy()
             self.table = torch.from_numpy(raw).to(self.device)
             props = torch.cuda.get_device_properties(self.device)
@@ -512,6 +524,12 @@ class PersistentEngine:
         self.aut_dfa_chunk = (torch.tensor(self.dfa_chunk, dtype=torch.int32, device=self.device)
                               if any(self.dfa_chunk) else None)
         self.min_dfa_chunk = min([c for c in self.dfa_chunk if c] or [0])
+        # chunk lengths follow the batch (one wave of the chunk launch) unless fixed
+        self.dfa_warps = 0
+        if self.aut_dfa_chunk is not None and dfa_chunk_bytes is None:
+            with torch.cuda.device(self.device):
+                self.dfa_warps = self.sm_count * int(
+                    lib.gbfsm_dfa_chunks_warps_per_sm(max(1, self.dfa_max_states)))
         self.fixed_chunk = -1 if chunk_bytes is None else max(0, int(chunk_bytes))
         if self.fixed_chunk > 0:
             self.fixed_chunk = max(self.fixed_chunk, MIN_CHUNK)
@@ -1029,7 +1047,8 @@ class GraphRunner:
                 "persistent_tasks": int(h[native.PLAN_PERSIST_TASKS]),
                 "fixup_tasks": int(h[native.PLAN_FIXUP_TASKS]),
                 "dfa_chunks": int(h[native.PLAN_DFA_CHUNKS]),
-                "dfa_fixups": int(h[native.PLAN_DFA_FIXUPS])}
+                "dfa_fixups": int(h[native.PLAN_DFA_FIXUPS]),
+                "dfa_chunk_bytes": int(h[native.PLAN_DFA_CHUNK_BYTES])}
 
     def verdicts(self):
         """(flags, lens, examined) of the last replay, once it has finished."""

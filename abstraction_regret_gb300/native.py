@@ -136,6 +136,7 @@ class BatchPlanArgs(ctypes.Structure):
         ("aut_ids", ctypes.c_void_p), ("aut_class", ctypes.c_void_p),
         ("aut_dfa_chunk", ctypes.c_void_p),
         ("lane_warps", ctypes.c_int32), ("persist_warps", ctypes.c_int32),
+        ("dfa_warps", ctypes.c_int32),
         ("min_chunk", ctypes.c_int32), ("fixed_chunk", ctypes.c_int32),
         ("n_slices", ctypes.c_int32), ("shrink", ctypes.c_float),
         ("slice_first", ctypes.c_int32 * (PLAN_MAX_SLICES + 1)),
@@ -156,7 +157,8 @@ PLAN_NFA_WHOLE, PLAN_NFA_WARP, PLAN_NFA_LANES, PLAN_DFA = 0, 1, 2, 3
 PLAN_HEADER_WORDS = 64
 (PLAN_STATUS, PLAN_LANE_CHUNKS, PLAN_CHUNKS, PLAN_LANE_FIRST, PLAN_LANE_TASKS,
  PLAN_PERSIST_TASKS, PLAN_FIXUP_TASKS, PLAN_LANE_BYTES, PLAN_WARP_BYTES, PLAN_OVERFLOW,
- PLAN_WHOLE, PLAN_DFA_INPUTS, PLAN_DFA_CHUNKS, PLAN_DFA_FIXUPS) = range(14)
+ PLAN_WHOLE, PLAN_DFA_INPUTS, PLAN_DFA_CHUNKS, PLAN_DFA_FIXUPS,
+ PLAN_DFA_CHUNK_BYTES) = range(15)
 PLAN_SLICES = 16
 
 (TASK_WHOLE, TASK_CHUNK, TASK_FIXUP, TASK_LANES, TASK_DFA_GROUP, TASK_DFA_CHUNK,
@@ -221,6 +223,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbfsm_probe_copy": (ctypes.c_int, [_vp, _vp, _sz, _i32, _vp]),
     "gbfsm_pageable_access": (_i32, []),
     "gbfsm_gather_inputs": (ctypes.c_int, [_vp, _vp, _i32, _vp, _vp]),
+    "gbfsm_dfa_chunks_warps_per_sm": (_i32, [_i32]),
     "gbfsm_dfa_chunks_run": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp,
                                             _P(ChunkIO), _i32, _vp, _vp, _vp, _vp, _vp]),
 }

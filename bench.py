@@ -885,11 +885,11 @@ def c4_section(dev, steps: int) -> dict:
 
 def dfa_chunks_section(dev, steps: int) -> dict:
     """Chunked DFA walks (DFA_CHUNK / DFA_FIXUP tasks) against whole-input walks (one lane
-    per input) in one engine step, on the c2 DFA (4096 states, no accepting state):
-    64 inputs of 4 MiB (chunks of the engine's own length), and c2-sustained itself (4096
-    inputs of 64 KiB, which the engine runs whole) with 16 KiB chunks forced. Verdicts
-    and examined counts bit-exact against the oracle first; device time per step
-    (planning included)."""
+    per input) in one engine step, no accepting state: 64 inputs of 4 MiB on the c2 DFA
+    (4096 states); one 4 MiB input on a 16384-state DFA (the latency of a lone long
+    request); c2-sustained itself (4096 inputs of 64 KiB: the engine's own choice, which
+    runs them whole) and with 16 KiB chunks forced. Verdicts and examined counts
+    bit-exact against the oracle first; device time per step (planning included)."""
     import torch
 
     from abstraction_regret_gb300 import engine as E
@@ -897,16 +897,21 @@ def dfa_chunks_section(dev, steps: int) -> dict:
     from abstraction_regret_gb300.engine import GraphRunner, PersistentEngine
     from oracle import oracle as O
 
+    from abstraction_regret_gb300.automata import random_dfa
+
     c2 = W.c2("sustained")
-    dfa = c2.automata[0]
     long_n, long_len = 64, 4 << 20
+    big = random_dfa(16384, accept_prob=0.0, seed=17)
     cases = {
-        "long_4MiB": (W.offsets_of(np.full(long_n, long_len, dtype=np.int64)),
+        "long_4MiB": (c2.automata[0], W.offsets_of(np.full(long_n, long_len, dtype=np.int64)),
                       W.uniform_bytes([1, 3], long_n * long_len), None),
-        "c2_sustained": (c2.offsets, c2.data, 16 << 10),
+        "one_4MiB_16384_states": (big, np.array([0, long_len], np.int64),
+                                  W.uniform_bytes([1, 5], long_len), None),
+        "c2_sustained": (c2.automata[0], c2.offsets, c2.data, None),
+        "c2_sustained_16KiB": (c2.automata[0], c2.offsets, c2.data, 16 << 10),
     }
     out = {}
-    for name, (offsets, data, forced) in cases.items():
+    for name, (dfa, offsets, data, forced) in cases.items():
         of, ol, oe = O.dfa_batch(dfa, data, offsets)
         row = {"inputs": int(len(offsets) - 1), "bytes": int(offsets[-1])}
         for mode, chunk in (("chunked", forced), ("whole", 0)):
@@ -929,12 +934,13 @@ def dfa_chunks_section(dev, steps: int) -> dict:
             r.stream.synchronize()
             row[mode] = {"ms": ms, "GBps": int(offsets[-1]) / (ms * 1e-3) / 1e9,
                          "dfa_chunks": info.get("dfa_chunks", 0),
-                         "chunk_bytes": int(eng.dfa_chunk[0]),
+                         "min_chunk_bytes": int(eng.dfa_chunk[0]),
+                         "batch_chunk_bytes": info.get("dfa_chunk_bytes", 0),
                          "phases_ms": {k: ev[0].elapsed_time(ev[1]) for k, ev in phases.items()
                                        if len(ev) >= 2}}
             del r, eng
         row["speedup"] = row["whole"]["ms"] / row["chunked"]["ms"]
-        row["overlap_cap_bytes"] = E.dfa_overlap_bytes(dfa.num_states)
+        row["states"] = int(dfa.num_states)
         out[name] = row
     return out
 
@@ -996,9 +1002,15 @@ def serving_section(dev, n_requests: int, slo_ms: float) -> dict:
         eng = engine if variant == "live" else PersistentEngine(base.automata, dev)
         pinned = torch.from_numpy(base.pool).pin_memory()
         runs, first = [], None
-        for rate in (8000.0, 32000.0, None):
+        # the sustained trace also runs its first 2000 requests at lower rates, to find
+        # where every-byte-examined load meets the SLO
+        rates = (8000.0, 32000.0, None) + ((2000.0, 500.0) if variant == "sustained" else ())
+        for rate in rates:
             # the same requests; only the arrival times scale with the rate
-            tr = dataclasses.replace(base, arrivals=base.arrivals / (rate or 1.0))
+            k = n_requests if rate is None or rate >= 8000.0 else min(n_requests, 2000)
+            tr = dataclasses.replace(base, arrivals=base.arrivals[:k] / (rate or 1.0),
+                                     aut_ids=base.aut_ids[:k], starts=base.starts[:k],
+                                     lengths=base.lengths[:k])
             srv = Server(engine=eng, slots=3, batch_bytes=256 << 20, max_requests=4096,
                          zero_copy=True)
             warm = dataclasses.replace(tr, aut_ids=tr.aut_ids[:256], arrivals=tr.arrivals[:256],
@@ -1012,7 +1024,7 @@ def serving_section(dev, n_requests: int, slo_ms: float) -> dict:
                     want = O.verdicts(base.automata[a], [bytes(data)])[0]
                     if (int(f[i]), int(l[i])) != (int(want[0]), int(want[1])):
                         raise SystemExit(f"serving {variant}: request {i} differs from the oracle")
-            elif not (np.array_equal(f, first[0]) and np.array_equal(l, first[1])):
+            elif not (np.array_equal(f, first[0][:k]) and np.array_equal(l, first[1][:k])):
                 raise SystemExit(f"serving {variant} at {rate}/s: verdicts changed")
             d = st.as_dict()
             d.update({"rate_per_s": rate if rate else "all at t=0",

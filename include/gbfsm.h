@@ -256,8 +256,9 @@ typedef struct gbfsm_automaton {
     int32_t kind;          /* 0 = NFA, 1 = DFA */
     int32_t technique;     /* NFA: GBFSM_TECH_WARP or GBFSM_TECH_COMPACT */
     int32_t list_capacity; /* NFA compact list capacity (<= the launch's capacity) */
-    int32_t dfa_overlap;   /* DFA: bytes a DFA_CHUNK task's exact walk continues past its
-                              chunk's end (0 = none; every chunk then links by a walk) */
+    int32_t dfa_overlap;   /* DFA: the most bytes a DFA_CHUNK task's exact walk continues
+                              past its chunk's end, never past the next chunk's end (0 =
+                              none: every chunk then links by a serial walk) */
     gbfsm_nfa_dev nfa;     /* valid when kind == 0 */
     gbfsm_dfa_dev dfa;     /* valid when kind == 1 */
 } gbfsm_automaton;
@@ -415,8 +416,8 @@ gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_autom
 #define GBFSM_PLAN_NFA_LANES 2 /* NFA: every input cut into lane chunks (the automaton
                                   needs the lane tables) */
 #define GBFSM_PLAN_DFA 3       /* DFA inputs, 32 per task, one walk per lane; inputs of at
-                                  least twice the DFA's aut_dfa_chunk bytes are cut into
-                                  DFA chunks instead */
+                                  least two DFA chunks (gbfsm_batch_plan_args.aut_dfa_chunk,
+                                  dfa_warps) are cut into DFA chunks instead */
 
 /* Words of the plan header (int32, device). */
 #define GBFSM_PLAN_HEADER_WORDS 64
@@ -437,6 +438,8 @@ gbfsm_status gbfsm_lanes_run_range(const gbfsm_automaton *table, int32_t n_autom
 #define GBFSM_PLAN_DFA_CHUNKS 12   /* task_count of the DFA chunk launch (chunks of long DFA
                                       inputs, after the lane and warp chunks) */
 #define GBFSM_PLAN_DFA_FIXUPS 13   /* task_count of the DFA fix-up launch */
+#define GBFSM_PLAN_DFA_CHUNK_BYTES 14 /* the batch's DFA chunk length before each DFA's
+                                         minimum (0: from aut_dfa_chunk alone) */
 #define GBFSM_PLAN_SLICES 16       /* {first, count} LANES task range of slice k at
                                       16 + 2k, for gbfsm_lanes_run_range */
 #define GBFSM_PLAN_MAX_SLICES 16
@@ -449,11 +452,18 @@ typedef struct gbfsm_batch_plan_args {
                                  offsets[i + 1] */
     const int32_t *aut_ids;   /* device [n_inputs] or NULL (all automaton 0) */
     const int32_t *aut_class; /* device [n_automata]: GBFSM_PLAN_* */
-    const int32_t *aut_dfa_chunk; /* device [n_automata] or NULL: DFA chunk bytes (0 = run
-                                     the DFA's inputs whole) */
+    const int32_t *aut_dfa_chunk; /* device [n_automata] or NULL: shortest DFA chunk of each
+                                     automaton, bytes (0 = run the DFA's inputs whole) */
     int32_t lane_warps;       /* resident warps of the lane launch (SMs x
                                  gbfsm_lanes_warps_per_sm) */
     int32_t persist_warps;    /* resident warps of the persistent launch */
+    int32_t dfa_warps;        /* resident warps of the DFA chunk launch (SMs x
+                                 gbfsm_dfa_chunks_warps_per_sm), or 0. An input of DFA a is
+                                 cut into chunks of max(aut_dfa_chunk[a], B / dfa_warps)
+                                 bytes, B the bytes of the batch's DFA inputs that hold two
+                                 chunks of their own minimum, when it holds two of them:
+                                 short chunks when few long inputs leave warps idle, one
+                                 wave of chunks otherwise */
     int32_t min_chunk;        /* shortest chunk (bytes) */
     int32_t fixed_chunk;      /* > 0: every chunk size; 0: chosen; < 0: never chunk */
     int32_t n_slices;         /* 0 or 1: one lane range; else inputs cut into slices at
@@ -486,6 +496,10 @@ size_t gbfsm_batch_plan_scratch_bytes(int32_t n_inputs);
 /* Enqueue the planning launches on `stream`. Validates the arguments on the host;
  * device-side failures (capacity, automaton ids) are reported in the header's status. */
 gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *args, void *stream);
+
+/* Resident warps per SM of gbfsm_dfa_chunks_run for DFAs of up to max_states states (its
+ * shared scratch grows with them); 0 when the query fails. */
+int32_t gbfsm_dfa_chunks_warps_per_sm(int32_t max_states);
 
 /* Run DFA_CHUNK or DFA_FIXUP tasks (others are skipped): min(*task_count, max_tasks)
  * tasks of `tasks` when task_count is non-NULL, else max_tasks. A step runs the DFA_CHUNK

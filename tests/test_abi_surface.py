@@ -60,8 +60,8 @@ def test_python_binding_covers_the_header(lib):
     assert lib.gbfsm_abi_version() == native.ABI_VERSION
 
 
-PLAN_FIELDS = ("aut_dfa_chunk", "lane_warps", "slice_first", "cap_chunks",
-               "cap_dfa_chunk_tasks", "cap_dfa_fixup_tasks", "chunks", "tasks_dfa_chunk",
+PLAN_FIELDS = ("aut_dfa_chunk", "lane_warps", "dfa_warps", "n_slices", "slice_first",
+               "cap_chunks", "cap_dfa_chunk_tasks", "cap_dfa_fixup_tasks", "chunks", "tasks_dfa_chunk",
                "tasks_dfa_fixup", "dfa_latch", "input_ids", "scratch")
 
 
@@ -80,7 +80,7 @@ def test_struct_layouts_match_the_header(tmp_path):
     lines.append('  printf("static %u\\n", GBFSM_STATIC_SCRATCH_BYTES);')
     for name in ("STATUS", "LANE_CHUNKS", "CHUNKS", "LANE_FIRST", "LANE_TASKS",
                  "PERSIST_TASKS", "FIXUP_TASKS", "LANE_BYTES", "WARP_BYTES", "OVERFLOW",
-                 "WHOLE", "DFA_INPUTS", "DFA_CHUNKS", "DFA_FIXUPS", "SLICES", "MAX_SLICES", "HEADER_WORDS", "NFA_WHOLE",
+                 "WHOLE", "DFA_INPUTS", "DFA_CHUNKS", "DFA_FIXUPS", "DFA_CHUNK_BYTES", "SLICES", "MAX_SLICES", "HEADER_WORDS", "NFA_WHOLE",
                  "NFA_WARP", "NFA_LANES", "DFA"):
         lines.append(f'  printf("PLAN_{name} %d\\n", GBFSM_PLAN_{name});')
     for name in ("DFA_GROUP", "DFA_CHUNK", "DFA_FIXUP"):

@@ -43,7 +43,7 @@ def _collapse(trans, n, data, b, e):
     return -1, 0
 
 
-def _chunk(dfa, data, length, b, e, index, overlap, next_p=None):
+def _chunk(dfa, data, length, b, e, index, overlap, next_p=None, e_next=None):
     trans, acc = dfa.trans, dfa.accept
     a = -1
     s = 0
@@ -53,16 +53,18 @@ def _chunk(dfa, data, length, b, e, index, overlap, next_p=None):
             a = 0
     else:
         p, s = _collapse(trans, dfa.num_states, data, b, e)
-    ov_len, ov_acc = 0, -1
+    ov_len, ov_acc, ov_state = 0, -1, 0
     if p >= 0 and a < 0:
         s, a = _span(trans, acc, s, data, p, e)
         if a < 0:
             ov_end = min(e + max(overlap, 0), length)
-            if next_p is not None:  # adaptive: stop at the next chunk's collapse
-                ov_end = min(ov_end, max(next_p, e)) if next_p >= 0 else e
-            _, ov_acc = _span(trans, acc, s, data, e, ov_end)
+            if e_next is not None:  # never past the next chunk's end
+                ov_end = min(ov_end, e_next)
+            if next_p is not None and next_p >= 0:  # adaptive: stop at its collapse
+                ov_end = min(ov_end, max(next_p, e))
+            ov_state, ov_acc = _span(trans, acc, s, data, e, ov_end)
             ov_len = (ov_acc if ov_acc >= 0 else ov_end) - e
-    return dict(p=p, acc=a, end_state=s, ov_len=ov_len, ov_acc=ov_acc)
+    return dict(p=p, acc=a, end_state=s, ov_len=ov_len, ov_acc=ov_acc, ov_state=ov_state)
 
 
 def _fixup(dfa, data, length, bounds, recs):
@@ -72,6 +74,7 @@ def _fixup(dfa, data, length, bounds, recs):
         return 1, r0["acc"], r0["acc"]
     s = r0["end_state"]
     prev_ok, prev_ov_len, prev_ov_acc = True, r0["ov_len"], r0["ov_acc"]
+    prev_ov_state = r0["ov_state"]
     for k in range(1, len(recs)):
         if prev_ok and prev_ov_acc >= 0:
             return 1, prev_ov_acc, prev_ov_acc
@@ -86,10 +89,14 @@ def _fixup(dfa, data, length, bounds, recs):
                 return 1, r["acc"], r["acc"]
             s = r["end_state"]
             prev_ok, prev_ov_len, prev_ov_acc = True, r["ov_len"], r["ov_acc"]
+            prev_ov_state = r["ov_state"]
         else:
-            s, a = _span(trans, acc, s, data, b, e)
-            if a >= 0:
-                return 1, a, a
+            if prev_ok and prev_ov_len == e - b:
+                s = prev_ov_state  # the previous overlap covered the whole chunk
+            else:
+                s, a = _span(trans, acc, s, data, b, e)
+                if a >= 0:
+                    return 1, a, a
             prev_ok = False
     return 0, 0, length
 
@@ -104,7 +111,8 @@ def chunked_verdict(dfa, data: np.ndarray, chunk: int, overlap: int, adaptive: b
     if adaptive:  # the collapse positions the chunks publish
         for k in range(1, cnt):
             nxt[k - 1] = _collapse(dfa.trans, dfa.num_states, data, *bounds[k])[0]
-    recs = [_chunk(dfa, data, length, b, e, k, overlap, nxt[k])
+    ends = [e for _, e in bounds[1:]] + [None]
+    recs = [_chunk(dfa, data, length, b, e, k, overlap, nxt[k], ends[k] if adaptive else None)
             for k, (b, e) in enumerate(bounds)]
     return _fixup(dfa, data, length, bounds, recs), recs
 
@@ -166,6 +174,21 @@ def test_random_dfas(n, accept_prob, overlap, adaptive):
     inputs = [rng.integers(0, 256, int(m), dtype=np.uint8)
               for m in rng.integers(512, 4000, 12)]
     _check(dfa, inputs, 256, overlap, adaptive)
+
+
+@pytest.mark.parametrize("overlap", [300, 10_000])
+def test_overlap_covers_chunks_that_never_collapse(overlap):
+    """Permutation DFA (no collapse without the alarm byte): an overlap of a whole chunk
+    carries the true state over it, so the fix-up need not walk it."""
+    dfa = _alarm_dfa(24, seed=1, permutation=True)
+    rng = np.random.default_rng(7)
+    x = rng.integers(0, 255, 2000, dtype=np.uint8)
+    x[700] = 255  # chunk 2 collapses at the alarm byte; chunks 1, 3.. never do
+    x[1900] = 255
+    (f, ln, ex), recs = chunked_verdict(dfa, x, 256, overlap, adaptive=True)
+    want = O.dfa_batch(dfa, x, np.array([0, x.size], np.int64))
+    assert (f, ln, ex) == (want[0][0], want[1][0], want[2][0])
+    assert any(r["p"] == -1 for r in recs[1:])
 
 
 def test_adaptive_overlap_links_exactly_at_the_collapse():

@@ -95,18 +95,18 @@ def _boundary_inputs(chunk: int, lengths, seed: int):
 @pytest.mark.parametrize("permutation", [False, True])
 def test_accepts_around_chunk_boundaries(permutation):
     dfa = _alarm_dfa(64, seed=1, permutation=permutation)
-    eng = PersistentEngine([dfa])
     chunk = E.dfa_chunk_length(64)
+    eng = PersistentEngine([dfa], dfa_chunk_bytes=chunk)  # fixed: the boundaries are known
     inputs = _boundary_inputs(chunk, [2 * chunk, 5 * chunk + 123, 9 * chunk - 7], seed=2)
     flags = _run_and_check(eng, [0] * len(inputs), inputs)
     assert 0 < int(flags.sum()) < len(inputs)
 
 
 def test_no_overlap_links_every_chunk_by_a_gap_walk(monkeypatch):
-    monkeypatch.setattr(E, "DFA_OVERLAP_PER_STATE", 0)
+    monkeypatch.setattr(E, "DFA_OVERLAP_CHUNKS", 0.0)
     dfa = _alarm_dfa(200, seed=3, permutation=False)
-    eng = PersistentEngine([dfa])
     chunk = E.dfa_chunk_length(200)
+    eng = PersistentEngine([dfa], dfa_chunk_bytes=chunk)
     inputs = _boundary_inputs(chunk, [3 * chunk + 5, 6 * chunk], seed=4)
     _run_and_check(eng, [0] * len(inputs), inputs)
 
@@ -164,8 +164,8 @@ def test_early_accept_stops_later_chunks():
     chunks (their records say p = -2); verdicts stay exact, including an input whose
     accept lies in a later chunk's overlap and one with no accept."""
     dfa = _alarm_dfa(64, seed=5, permutation=False)
-    eng = PersistentEngine([dfa])
     chunk = E.dfa_chunk_length(64)
+    eng = PersistentEngine([dfa], dfa_chunk_bytes=chunk)
     length = 16 * chunk
     rng = np.random.default_rng(6)
     inputs = []
@@ -187,3 +187,24 @@ def test_early_accept_stops_later_chunks():
     assert first.size == 16 and (p_later == -2).mean() >= 0.9, p_later
     p_none = recs[n_lane:][chunks[n_lane:]["input"] == 3][1:, 0]
     assert (p_none >= 0).all()
+
+
+def test_chunk_length_follows_the_batch():
+    """Few long inputs get the DFA's shortest chunks; enough long inputs to fill the chunk
+    launch get longer chunks (one wave), and verdicts stay exact either way."""
+    dfa = random_dfa(256, accept_prob=0.0, seed=13)
+    eng = PersistentEngine([dfa])
+    minimum = E.dfa_chunk_length(256)
+    assert eng.dfa_warps > 0
+    rng = np.random.default_rng(14)
+    few = [rng.integers(0, 256, 8 * minimum, dtype=np.uint8).tobytes() for _ in range(2)]
+    _run_and_check(eng, [0] * 2, few, min_dfa_chunks=16)
+    h = eng._dplan.h_header.numpy()
+    assert int(h[native.PLAN_DFA_CHUNK_BYTES]) <= minimum
+    n = -(-2 * minimum * eng.dfa_warps // (2 << 20))  # about two chunk-lengths per warp
+    many = [rng.integers(0, 256, 2 << 20, dtype=np.uint8).tobytes() for _ in range(n)]
+    _run_and_check(eng, [0] * n, many)
+    h = eng._dplan.h_header.numpy()
+    target = int(h[native.PLAN_DFA_CHUNK_BYTES])
+    assert target > minimum
+    assert int(h[native.PLAN_DFA_CHUNKS]) <= eng.dfa_warps  # one wave
