@@ -37,18 +37,16 @@ def batch_results(
     transfer_ms: float = 0.0,
 ) -> list[Result]:
     """One :class:`Result` per input, with the batch's times on the first one only."""
-    out = []
-    for i in range(len(flags)):
-        first = i == 0
-        out.append(
-            Result(
-                accepted=bool(flags[i]),
-                match_len=int(lens[i]),
-                kernel_ms=kernel_ms if first else 0.0,
-                total_ms=(kernel_ms + transfer_ms) if first else 0.0,
-                transfer_ms=transfer_ms if first else 0.0,
-            )
-        )
+    f = flags.tolist() if hasattr(flags, "tolist") else [bool(x) for x in flags]
+    m = lens.tolist() if hasattr(lens, "tolist") else [int(x) for x in lens]
+    # positional construction of plain Python values: about half the time of keyword
+    # construction for large batches
+    out = [Result(a != 0, b) for a, b in zip(f, m)]
+    if out:
+        first = out[0]
+        first.kernel_ms = kernel_ms
+        first.total_ms = kernel_ms + transfer_ms
+        first.transfer_ms = transfer_ms
     return out
 
 

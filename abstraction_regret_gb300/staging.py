@@ -35,6 +35,34 @@ def _address(b) -> int:
     return int(np.frombuffer(b, dtype=np.uint8).ctypes.data)
 
 
+def _bytes_data_offset() -> int | None:
+    """Offset of a ``bytes`` object's data from its ``id()`` in this interpreter (the
+    object header; the same for every ``bytes``), or None where ``id()`` is not the
+    object's address or the offset differs between probes."""
+    probes = [b"", b"x", bytes(100), bytes(range(256)) * 40]
+    offs = {(ctypes.cast(p, ctypes.c_void_p).value or 0) - id(p) for p in probes}
+    if len(offs) != 1:
+        return None
+    off = offs.pop()
+    return off if 0 < off < 256 else None
+
+
+_BYTES_OFFSET = _bytes_data_offset()
+
+
+def addresses(inputs, out: np.ndarray) -> None:
+    """Write the data address of every input into ``out`` (int64). A batch of plain
+    ``bytes`` takes the addresses from ``id()`` at once (a few microseconds per thousand
+    inputs instead of one ``ctypes`` call each)."""
+    n = len(inputs)
+    if _BYTES_OFFSET is not None and all(type(b) is bytes for b in inputs):
+        out[:n] = np.fromiter(map(id, inputs), dtype=np.int64, count=n)
+        out[:n] += _BYTES_OFFSET
+        return
+    for i, b in enumerate(inputs):
+        out[i] = _address(b)
+
+
 def _grow(cap: int, need: int) -> int:
     cap = max(cap, 1 << 12)
     while cap < need:
@@ -102,9 +130,7 @@ class Staging:
         if n and total >= GATHER_MIN_BYTES and self._can_gather():
             # the GPU reads each input where it lies; the caller keeps ``inputs`` alive
             # until the stream has passed this copy (the executors synchronise first)
-            h_ptr = self._h_ptr.numpy()
-            for i, b in enumerate(inputs):
-                h_ptr[i] = _address(b)
+            addresses(inputs, self._h_ptr.numpy())
             from . import native
 
             with torch.cuda.stream(stream):

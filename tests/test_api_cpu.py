@@ -342,3 +342,31 @@ def test_per_input_lane_chunk_sizes():
         c = p.chunks[p.chunks["input"] == i]
         assert len(c) == -(-10000 // size)
         assert (c["end"] - c["begin"]).max() <= size
+
+
+def test_input_addresses_equal_ctypes_for_every_input_kind():
+    """The gather path's address table: plain bytes through id() and the header offset,
+    anything else through the buffer protocol; both give each input's own storage."""
+    from abstraction_regret_gb300 import staging as S
+
+    plain = [bytes(k) for k in range(50)] + [b"", b"abc" * 100]
+    mixed = plain + [bytearray(b"xyz"), memoryview(b"0123456789")[2:7]]
+    for inputs in (plain, mixed):
+        out = np.zeros(len(inputs), np.int64)
+        S.addresses(inputs, out)
+        assert [int(a) for a in out] == [S._address(b) for b in inputs]
+
+
+def test_batch_results_values_and_timing_convention():
+    """Verdicts from arrays or lists; the batch's times on the first result only."""
+    from abstraction_regret_gb300.result import Result, batch_results
+
+    for flags, lens in ((np.array([1, 0, 1], np.int32), np.array([3, 0, 7], np.int32)),
+                        ([True, False, True], [3, 0, 7])):
+        res = batch_results(flags, lens, 2.0, 0.5)
+        assert [(r.accepted, r.match_len) for r in res] == [(True, 3), (False, 0), (True, 7)]
+        assert all(type(r.accepted) is bool and type(r.match_len) is int for r in res)
+        assert (res[0].kernel_ms, res[0].total_ms, res[0].transfer_ms) == (2.0, 2.5, 0.5)
+        assert all(r.kernel_ms == r.total_ms == r.transfer_ms == 0.0 for r in res[1:])
+        assert isinstance(res[0], Result)
+    assert batch_results([], [], 1.0) == []
