@@ -343,14 +343,13 @@ __device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
     return ~(t | x) & 0x80808080u;
 }
 
-// Byte markers of the first min(k, 8) bytes of an 8-byte label pair (lo: bytes 0..3,
-// hi: bytes 4..7), from one 64-bit shift (k >= 0; shr.b64 clamps 64 to an empty mask).
-__device__ __forceinline__ void first_bytes8(int k, uint32_t &lo, uint32_t &hi) {
-    const uint32_t shift = 64u - 8u * (uint32_t)min(k, 8);
-    uint64_t m;
-    asm("shr.b64 %0, %1, %2;" : "=l"(m) : "l"(0x8080808080808080ull), "r"(shift));
-    lo = (uint32_t)m;
-    hi = (uint32_t)(m >> 32);
+// Byte markers of the first k (< 0: none, >= 4: all four) bytes of a word.
+__device__ __forceinline__ uint32_t first_bytes(int k) {
+    // shr.b32 clamps shift counts above 32 to 32, which yields 0 (k <= 0)
+    const uint32_t shift = 32u - 8u * (uint32_t)min(max(k, 0), 4);
+    uint32_t r;
+    asm("shr.b32 %0, %1, %2;" : "=r"(r) : "r"(0x80808080u), "r"(shift));
+    return r;
 }
 
 // Markers (bit 7 of byte j of word w: edge 4w + j) of the labels of a fast-form record
@@ -359,19 +358,15 @@ __device__ __forceinline__ void first_bytes8(int k, uint32_t &lo, uint32_t &hi) 
 __device__ __forceinline__ int label_matches(const uint4 &r, uint32_t sym4,
                                              const uint2 *__restrict__ ext, uint32_t (&m)[4]) {
     const int deg = (int)lane_degree(r.x);
-    uint32_t k0, k1;
-    first_bytes8(deg, k0, k1);
-    m[0] = zero_bytes(r.z ^ sym4) & k0;
-    m[1] = zero_bytes(r.w ^ sym4) & k1;
+    m[0] = zero_bytes(r.z ^ sym4) & first_bytes(deg);
+    m[1] = zero_bytes(r.w ^ sym4) & first_bytes(deg - 4);
     m[2] = 0u;
     m[3] = 0u;
     int c = __popc(m[0]) + __popc(m[1]);
     if (deg > 8) {
         const uint2 h = __ldg(ext + (r.x & GBFSM_LANE_STATE_MASK));
-        uint32_t k2, k3;
-        first_bytes8(deg - 8, k2, k3);
-        m[2] = zero_bytes(h.x ^ sym4) & k2;
-        m[3] = zero_bytes(h.y ^ sym4) & k3;
+        m[2] = zero_bytes(h.x ^ sym4) & first_bytes(deg - 8);
+        m[3] = zero_bytes(h.y ^ sym4) & first_bytes(deg - 12);
         c += __popc(m[2]) + __popc(m[3]);
     }
     return c;
@@ -380,19 +375,23 @@ __device__ __forceinline__ int label_matches(const uint4 &r, uint32_t sym4,
 // Edge of the lowest remaining marker of m (edge 4w + j of the row starting at rb for
 // bit 7 of byte j of word w), cleared from m. m must have a marker.
 __device__ __forceinline__ uint32_t pop_match(uint32_t (&m)[4], uint32_t rb) {
-    // markers of edges 0..7 (almost every match) or 8..15 as one 64-bit word each
-    const bool low = (m[0] | m[1]) != 0u;
-    uint64_t w = low ? (((uint64_t)m[1] << 32) | m[0]) : (((uint64_t)m[3] << 32) | m[2]);
-    const uint32_t k = (uint32_t)(__ffsll((long long)w) - 1) >> 3;
-    w &= w - 1u;
-    if (low) {
-        m[0] = (uint32_t)w;
-        m[1] = (uint32_t)(w >> 32);
+    uint32_t w, off;
+    if (m[0] | m[1]) {  // edges 0..7: almost every match
+        const bool z0 = m[0] != 0u;
+        w = z0 ? m[0] : m[1];
+        off = z0 ? 0u : 4u;
+        const uint32_t rest = w & (w - 1u);
+        if (z0) m[0] = rest;
+        else m[1] = rest;
     } else {
-        m[2] = (uint32_t)w;
-        m[3] = (uint32_t)(w >> 32);
+        const bool z2 = m[2] != 0u;
+        w = z2 ? m[2] : m[3];
+        off = z2 ? 8u : 12u;
+        const uint32_t rest = w & (w - 1u);
+        if (z2) m[2] = rest;
+        else m[3] = rest;
     }
-    return rb + (low ? 0u : 8u) + k;
+    return rb + off + ((uint32_t)(__ffs(w) - 1) >> 3);
 }
 
 // The set becomes the distinct targets of the matched edges mk[0 .. nm) (nm <= kLaneSlots),
