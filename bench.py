@@ -262,8 +262,10 @@ def nfa_roofline(counts: dict, ms: float, onchip: dict | None) -> dict:
     lat = onchip.get("l2_latency_ns") if onchip else None
     sym = counts["examined"] / (ms * 1e-3) / 1e9
     bound_sym = counts["chains"] / lat if lat and counts["chains"] else None
+    smem = onchip.get("smem_GBps") if onchip else None
     return {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
             "frac": achieved / l2 if l2 else None, "algorithmic_bytes": int(algo),
+            "smem_peak": smem, "frac_of_smem_peak": achieved / smem if smem else None,
             "latency": {"chains": counts["chains"], "l2_latency_ns": lat,
                         "bound_Gsymbols_per_s": bound_sym, "achieved_Gsymbols_per_s": sym,
                         "frac": sym / bound_sym if bound_sym else None},
@@ -276,11 +278,18 @@ def dfa_roofline(examined: int, chains: int, ms: float, onchip: dict | None,
     table entry held on chip, so ``chains`` walks run at most chains / L2 latency symbols
     per second; the input stream (1 byte per symbol) against HBM beside it."""
     lat = onchip.get("l2_latency_ns") if onchip else None
+    l2 = onchip.get("l2_read_GBps") if onchip else None
     sym = examined / (ms * 1e-3) / 1e9
     bound = chains / lat if lat else None
+    # the bandwidth view: per examined symbol 1 input byte from HBM and one table entry
+    # (counted as 4 bytes, the reference's int32 table, and as a whole 32-byte L2 sector)
+    bw_bound = min(hbm / 1.0, l2 / 4.0) if l2 else hbm
     return {"bound": "latency", "achieved": sym, "peak": bound, "unit": "Gsymbols/s",
             "frac": sym / bound if bound else None, "chains": chains, "l2_latency_ns": lat,
             "algorithmic_bytes": 3 * int(examined),
+            "bandwidth": {"bound_Gsymbols_per_s": bw_bound, "frac": sym / bw_bound,
+                          "frac_at_32B_per_sector": sym / (l2 / 32.0) if l2 else None,
+                          "rule": "min(HBM/1 B, L2/4 B) per examined symbol"},
             "input_stream": {"achieved": sym, "peak": hbm, "unit": "GB/s",
                              "frac": sym / hbm},
             "peak_source": "chains / L2 dependent-load latency measured in this run "

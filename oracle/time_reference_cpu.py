@@ -8,7 +8,9 @@ registers ``reference`` and, for NFAs, ``bitmap``). It is imported from its chec
 this runs where the checkout is (the development container), not on the GPU machines.
 For each workload it times a fixed deterministic sample -- the first inputs of the batch,
 cut to a byte budget -- checks the verdicts against this repository's oracle, and prints
-one JSON line per (workload, technique) with the examined bytes per second.
+one JSON line per (workload, technique) with the examined bytes per second: on one core,
+and fanned out over one process per host core (inputs dealt round-robin; the worker
+processes are started and loaded before the clock starts).
 """
 
 from __future__ import annotations
@@ -25,6 +27,41 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
+
+
+_W = {}
+
+
+def _init(reference: str, automaton, inputs) -> None:
+    sys.path.insert(0, str(Path(reference) / "src"))
+    import gpufsm
+
+    _W.update(gpufsm=gpufsm, automaton=automaton, inputs=inputs)
+
+
+def _run(job):
+    tech, idx = job
+    res = _W["gpufsm"].run_batch(_W["automaton"], [_W["inputs"][i] for i in idx],
+                                 backend="cpu", technique=tech)
+    return [(i, r.accepted, r.match_len) for i, r in zip(idx, res)]
+
+
+def fan_out(reference: str, automaton, inputs, tech: str, procs: int):
+    """Seconds for all inputs over ``procs`` worker processes, and their verdicts."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    jobs = [(tech, list(range(k, len(inputs), procs))) for k in range(procs)]
+    with ctx.Pool(procs, initializer=_init, initargs=(reference, automaton, inputs)) as pool:
+        pool.map(_run, [(tech, []) for _ in range(procs)])  # every worker loaded
+        t0 = time.perf_counter()
+        parts = pool.map(_run, jobs)
+        dt = time.perf_counter() - t0
+    got = [None] * len(inputs)
+    for part in parts:
+        for i, a, m in part:
+            got[i] = (a, m)
+    return dt, got
 
 
 def sample(batch, budget: int, cap: int):
@@ -79,6 +116,14 @@ def main() -> int:
                               "examined_MBps": examined / dt / 1e6, "cores": 1,
                               "host": platform.processor() or platform.machine(),
                               "cpus": os.cpu_count()}), flush=True)
+            procs = os.cpu_count() or 1
+            dt, got = fan_out(args.reference, ref, inputs, tech, procs)
+            assert got == want, f"{name}/{tech}: the fan-out disagrees with the oracle"
+            print(json.dumps({"workload": name, "technique": tech, "inputs": len(inputs),
+                              "bytes": int(off[-1]), "examined": examined, "seconds": dt,
+                              "examined_MBps": examined / dt / 1e6, "cores": procs,
+                              "processes": procs, "host": platform.processor() or
+                              platform.machine(), "cpus": os.cpu_count()}), flush=True)
     return 0
 
 

@@ -221,10 +221,12 @@ def test_c1_full(variant):
 
 
 @pytest.mark.parametrize("variant", ["literal", "sustained"])
-def test_c2_full_or_bounded(variant):
-    b = W.c2(variant, n_inputs=4096 if variant == "literal" else 512)
+def test_c2_full(variant):
+    b = W.c2(variant)
+    assert b.n_inputs == 4096
     for tech in DFA_TECHS:
         _check_batch(b, _plain(tech))
+    _check_batch(b, _persistent)
 
 
 @pytest.mark.parametrize("variant", ["literal", "live", "sustained"])
@@ -234,7 +236,7 @@ def test_c3_full(variant):
     _check_batch(b, _plain("compact"))
 
 
-@pytest.mark.parametrize("variant", ["literal", "live"])
+@pytest.mark.parametrize("variant", ["literal", "live", "sustained"])
 def test_c4_all_pairs_one_launch(variant):
     b = W.c4(variant)
     assert b.n_inputs == 1024
