@@ -76,6 +76,10 @@ int lanes_warps_per_sm() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = -1;
     if (dev >= 0 && cached[dev] > 0) return cached[dev];
+    // the kernel uses no shared memory: ask for the largest L1 share of the unified
+    // L1/shared storage, where the lane records that miss in registers are gathered from
+    cudaFuncSetAttribute(lanes_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaGetLastError();
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, lanes_kernel, kLanesThreads, 0) !=
         cudaSuccess)
@@ -91,13 +95,14 @@ gbfsm_status launch_lanes(const gbfsm_automaton *table, int32_t n_automata,
                           const uint8_t *data, const int64_t *offsets,
                           const gbfsm_chunk_io &chunk_io, cudaStream_t stream) {
     if (n_tasks <= 0) return GBFSM_OK;
+    const int warps_per_sm = lanes_warps_per_sm();  // once per device: sets the L1 share
     ChunkIO io{chunk_io.chunks, static_cast<ChunkRecord *>(chunk_io.records),
                chunk_io.overflow_tasks, chunk_io.overflow_count, nullptr, chunk_io.n_chunks,
                chunk_io.aut_ids};
     const int warps_per_block = kLanesThreads / 32;
     int grid = (n_tasks + warps_per_block - 1) / warps_per_block;
     if (range) {  // at most one resident wave; the warps loop over the tasks
-        const int wave = sm_count() * (lanes_warps_per_sm() / warps_per_block);
+        const int wave = sm_count() * (warps_per_sm / warps_per_block);
         if (wave > 0 && grid > wave) grid = wave;
     }
     lanes_kernel<<<grid, kLanesThreads, 0, stream>>>(table, n_automata, tasks, n_tasks, range,

@@ -186,10 +186,13 @@ class DevicePlan:
     step (planning included) can be captured once and replayed for new inputs of the
     same sizes. ``slices`` (input indices where slices start, plus ``n_inputs``) gives
     each slice's lane tasks their own range in the header, for pipelined ingest.
+    ``lane_waves``: how many waves of the lane launch the lane chunks fill (1: one chunk
+    per resident lane; more: shorter chunks that the slices of a pipelined step hand to
+    whichever lanes are free as their bytes arrive).
     """
 
     def __init__(self, engine: PersistentEngine, n_inputs: int, total_bytes: int,
-                 slices=None, shrink: float = 0.0) -> None:
+                 slices=None, shrink: float = 0.0, lane_waves: int = 1) -> None:
         self.engine = engine
         dev = engine.device
         self.n = int(n_inputs)
@@ -198,7 +201,8 @@ class DevicePlan:
         if self.slices is not None and len(self.slices) - 1 > native.PLAN_MAX_SLICES:
             raise ValueError(f"at most {native.PLAN_MAX_SLICES} slices")
         self.shrink = float(shrink) if self.slices else 0.0
-        lw = engine.sm_count * engine.lane_warps_per_sm
+        self.lane_waves = max(1, int(lane_waves))
+        lw = engine.sm_count * engine.lane_warps_per_sm * self.lane_waves
         pw = engine.resident_warps
         fixed = engine.fixed_chunk
         n = max(self.n, 1)
@@ -284,7 +288,7 @@ class DevicePlan:
             a.dfa_latch = self.dfa_latch.data_ptr()
         a.cap_dfa_chunk_tasks = self.cap_dfa_chunks
         a.cap_dfa_fixup_tasks = self.cap_dfa_fixup
-        a.lane_warps = eng.sm_count * eng.lane_warps_per_sm
+        a.lane_warps = eng.sm_count * eng.lane_warps_per_sm * self.lane_waves
         a.persist_warps = eng.resident_warps
         a.dfa_warps = eng.dfa_warps
         a.min_chunk = MIN_CHUNK
@@ -900,7 +904,7 @@ class GraphRunner:
 
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
                  with_examined: bool = False, ingest: str = "copy", parts: int = 8,
-                 shrink: float = 0.75) -> None:
+                 shrink: float = 0.75, lane_waves: int = 1) -> None:
         """``ingest`` says how each replay moves the inputs from the pinned host buffer:
 
         * ``copy``: one copy-engine transfer, then planning and the launches;
@@ -912,7 +916,8 @@ class GraphRunner:
           later slices; the overflow pass and the fix-up then run once for the whole
           batch. Inputs of slice k of P get the whole batch's lane chunk size scaled by
           1 - shrink * k / P: a slice that arrives later has less time left, so its lanes
-          get shorter chunks.
+          get shorter chunks. ``lane_waves`` > 1 cuts the lane chunks shorter still, to
+          fill that many waves of the lane launch.
 
         ``kernel_only`` plans and runs the batch on the device copy of the inputs."""
         if ingest not in self.INGEST:
@@ -938,7 +943,8 @@ class GraphRunner:
                 hi = min(total_b, -(-int(offsets[b]) // 16) * 16)
                 self.slices.append((lo, hi))
                 lo = hi
-        self.plan = DevicePlan(engine, max(n, 1), total, slices=slice_first, shrink=shrink)
+        self.plan = DevicePlan(engine, max(n, 1), total, slices=slice_first, shrink=shrink,
+                               lane_waves=lane_waves if slice_first else 1)
         # the resident copy for kernel_only (no slices: every lane task in one range)
         self.kplan = DevicePlan(engine, max(n, 1), total) if self.slices else self.plan
         padded = max(16, -(-total // 16) * 16)

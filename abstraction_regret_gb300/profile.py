@@ -13,7 +13,10 @@ inputs stay larger than L2 where the case's kernel streams them:
 * ``c4-sustained``   the engine on c4-sustained (64 NFAs, 1024 inputs; lanes and
                      persistent launches);
 * ``dfa-long``       chunked DFA walks (``dfa_chunks_kernel``): 8 inputs of 2 MiB on
-                     the c2 DFA (4096 states, no accepting state).
+                     the c2 DFA (4096 states, no accepting state);
+* ``c5-live``        the serving loop over the c5 pool (16 NFAs, 16 DFAs): the first
+                     2000 requests of the live trace, all arriving at once (the oracle
+                     checks 100 of them).
 """
 
 from __future__ import annotations
@@ -40,6 +43,24 @@ def run(case: str, steps: int) -> None:
     from .executors import CudaDFAExecutor, CudaNFAExecutor
 
     dev = torch.device("cuda", torch.cuda.current_device())
+    if case == "c5-live":
+        from .serving import Server
+
+        k = 2000
+        t = W.c5(rate_per_s=1.0, n_requests=k, variant="live")
+        eng = PersistentEngine(t.automata, dev)
+        pinned = torch.from_numpy(t.pool).pin_memory()
+        for step in range(1 + steps):
+            srv = Server(engine=eng, slots=3, batch_bytes=256 << 20, max_requests=4096,
+                         zero_copy=True)
+            f, l, _, _ = srv.serve(t, time_scale=0.0, pinned_pool=pinned)
+            if step == 0:
+                for i in range(0, k, k // 100):
+                    a, data = t.request(i)
+                    want = O.verdicts(t.automata[a], [bytes(data)])[0]
+                    if (int(f[i]), int(l[i])) != (int(want[0]), int(want[1])):
+                        raise SystemExit(f"c5-live: request {i} differs from the oracle")
+        return
     if case in ("c1-live", "c4-sustained", "dfa-long"):
         if case == "c1-live":
             b = W.c1("live")
@@ -98,7 +119,7 @@ def run(case: str, steps: int) -> None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("case", choices=["c1-live", "c1-plain", "c2-sustained", "c4-sustained",
-                                     "dfa-long"])
+                                     "dfa-long", "c5-live"])
     ap.add_argument("--steps", type=int, default=2)
     args = ap.parse_args(argv)
     run(args.case, args.steps)
