@@ -904,7 +904,7 @@ class GraphRunner:
 
     def __init__(self, engine: PersistentEngine, aut_ids, data: np.ndarray, offsets: np.ndarray,
                  with_examined: bool = False, ingest: str = "copy", parts: int = 8,
-                 shrink: float = 0.75, lane_waves: int = 1) -> None:
+                 shrink: float = 0.0, lane_waves: int = 2) -> None:
         """``ingest`` says how each replay moves the inputs from the pinned host buffer:
 
         * ``copy``: one copy-engine transfer, then planning and the launches;
@@ -916,8 +916,11 @@ class GraphRunner:
           later slices; the overflow pass and the fix-up then run once for the whole
           batch. Inputs of slice k of P get the whole batch's lane chunk size scaled by
           1 - shrink * k / P: a slice that arrives later has less time left, so its lanes
-          get shorter chunks. ``lane_waves`` > 1 cuts the lane chunks shorter still, to
-          fill that many waves of the lane launch.
+          get shorter chunks. ``lane_waves`` > 1 cuts the lane chunks shorter, to fill
+          that many waves of the lane launch, so that each arriving slice finds free lanes.
+          Measured on c3-sustained (2.76 ms per step): 8 slices, no shrink, 2 waves; one
+          wave with shrink 0.75 took 2.81 ms, 4 waves 2.87 ms (per-chunk work grows: the
+          resident step takes 1.92 / 2.22 / 2.61 ms at 1 / 2 / 4 waves).
 
         ``kernel_only`` plans and runs the batch on the device copy of the inputs."""
         if ingest not in self.INGEST:

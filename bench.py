@@ -456,8 +456,8 @@ def main(argv=None) -> int:
         "zero_copy": "CUDA graph: tables H2D, kernels read the inputs from pinned host "
                      "memory over NVLink-C2C, verdicts D2H",
         "pipelined": "CUDA graph: the inputs copied H2D from pinned memory in 8 slices on "
-                     "a copy stream; each slice's lane tasks run on their own stream as "
-                     "soon as its bytes arrive (later slices with shorter lane chunks); "
+                     "a copy stream; each slice's lane tasks (chunks for two waves of the "
+                     "lane launch) run on their own stream as soon as its bytes arrive; "
                      "overflow pass and fix-up once for the batch; verdicts D2H"}
     paths = {}
     for name, r in runners.items():

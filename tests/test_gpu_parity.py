@@ -355,18 +355,21 @@ def test_dfa_table_split_over_a_cluster(states):
     assert f.tolist() == [1, 1] and l.tolist() == [0, 0]
 
 
-@pytest.mark.parametrize("ingest", ["copy", "zero_copy", "pipelined"])
+@pytest.mark.parametrize("ingest", ["copy", "zero_copy", "pipelined", "pipelined-shrink"])
 def test_graph_runner_ingest_paths(ingest):
     """A captured step (H2D, launches, D2H) gives the oracle's verdicts on every ingest
-    path, replayed twice; the pipelined path plans each slice on its own."""
+    path, replayed twice; the pipelined path plans each slice on its own (two lane waves
+    by default; one wave with later slices' chunks shrunk)."""
     import torch
 
     from abstraction_regret_gb300.engine import GraphRunner
 
     b = W.c3("live", n_inputs=192)
     eng = PersistentEngine(b.automata)
+    extra = {"shrink": 0.75, "lane_waves": 1} if ingest == "pipelined-shrink" else {}
+    ingest = ingest.split("-")[0]
     r = GraphRunner(eng, b.aut_ids, b.data, b.offsets, with_examined=True, ingest=ingest,
-                    parts=3)
+                    parts=3, **extra)
     of, ol, oe, _ = O.nfa_batch(b.automata[0], b.data, b.offsets)
     for _ in range(2):
         with torch.cuda.stream(r.stream):
