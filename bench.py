@@ -780,6 +780,17 @@ def reference_gpu_section(dev, steps: int) -> dict:
     return out
 
 
+def launch_phases(runner) -> dict:
+    """Device time of each launch of one engine step (CUDA events around each)."""
+    import torch
+
+    phases: dict = {}
+    with torch.cuda.stream(runner.stream):
+        runner.kernel_only(runner.stream, phases=phases)
+    runner.stream.synchronize()
+    return {k: ev[0].elapsed_time(ev[1]) for k, ev in phases.items() if len(ev) >= 2}
+
+
 def c1_section(dev, steps: int) -> dict:
     """c1: the 1024-state NFA on 64 inputs of 4 KiB (live and sustained random walks;
     the literal inputs die after about one byte), one engine step and one plain launch,
@@ -806,6 +817,7 @@ def c1_section(dev, steps: int) -> dict:
             raise SystemExit(f"c1-{variant}: engine differs from the oracle")
         with torch.cuda.stream(r.stream):
             ms = time_launches(lambda: r.kernel_only(r.stream), r.stream, steps, 3)
+        phases = launch_phases(r)
         plain = CudaNFAExecutor(nfa, "auto", dev)
         d_out = torch.zeros((3, b.n_inputs), dtype=torch.int32, device=dev)
         with torch.cuda.stream(r.stream):
@@ -816,6 +828,7 @@ def c1_section(dev, steps: int) -> dict:
             raise SystemExit(f"c1-{variant}: plain launch differs from the oracle")
         info = r.plan_info()
         out[variant] = {"engine_GBps": b.total_bytes / (ms * 1e-3) / 1e9, "engine_ms": ms,
+                        "phases_ms": phases,
                         "plain_GBps": b.total_bytes / (plain_ms * 1e-3) / 1e9,
                         "plain_ms": plain_ms, "offered_bytes": int(b.total_bytes),
                         "checked": int(f.size),
@@ -864,6 +877,7 @@ def c4_section(dev, steps: int) -> dict:
                 raise SystemExit(f"c4-{variant}: automaton {k} differs from the oracle")
         with torch.cuda.stream(r.stream):
             ms = time_launches(lambda: r.kernel_only(r.stream), r.stream, steps, 3)
+        phases = launch_phases(r)
         # plain: one launch per automaton (its 16 inputs), back to back on one stream
         plains, subs = [], []
         for k, a in enumerate(b.automata):
@@ -889,6 +903,7 @@ def c4_section(dev, steps: int) -> dict:
 
         out[variant] = {"offered_GBps": b.total_bytes / (ms * 1e-3) / 1e9,
                         "examined_GBps": int(ex.sum()) / (ms * 1e-3) / 1e9, "ms": ms,
+                        "phases_ms": phases, "plan": r.plan_info(),
                         "plain_per_automaton_ms": plain_ms,
                         "speedup_vs_plain_per_automaton": plain_ms / ms,
                         "offered_bytes": int(b.total_bytes), "checked": int(f.size),

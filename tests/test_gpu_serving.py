@@ -96,3 +96,31 @@ def test_live_trace_served_alone_and_in_the_mix():
         a, data = trace.request(int(i))
         f, l, _, _, _ = engine.run_requests([a], [bytes(data)])
         assert (int(f[0]), int(l[0])) == want[i]
+
+
+def test_sustained_trace_chunks_long_dfa_requests():
+    """The sustained trace (every accept bit cleared, every byte examined): long DFA
+    requests are walked in chunks inside the serving batches, and every verdict and the
+    examined total equal the oracle's."""
+    pool = W.c5_pool()
+    trace = W.c5(rate_per_s=20000.0, n_requests=300, pool_bytes=1 << 24, automata=pool,
+                 variant="sustained", walks_per_nfa=2)
+    engine = PersistentEngine(trace.automata)
+    assert engine.aut_dfa_chunk is not None
+    srv = Server(engine=engine, slots=2, batch_bytes=64 << 20, max_requests=256,
+                 zero_copy=True)
+    flags, lens, _, stats = srv.serve(trace, time_scale=0.25)
+    examined = 0
+    long_dfa = 0
+    for i in range(len(trace.aut_ids)):
+        a, data = trace.request(i)
+        d, off = O.flatten([bytes(data)])
+        if hasattr(trace.automata[a], "trans"):
+            f, l, e = O.dfa_batch(trace.automata[a], d, off)
+            long_dfa += len(data) >= 2 * engine.dfa_chunk[a]
+        else:
+            f, l, e, _ = O.nfa_batch(trace.automata[a], d, off)
+        assert (int(flags[i]), int(lens[i])) == (int(f[0]), int(l[0])), i
+        examined += int(e[0])
+    assert long_dfa > 0
+    assert stats.examined_bytes == examined == stats.offered_bytes
