@@ -298,8 +298,8 @@ gbfsm_status gbfsm_batch_plan(const gbfsm_batch_plan_args *a, void *stream) {
         for (int k = 0; k < a->n_slices; ++k)
             if (a->slice_first[k + 1] < a->slice_first[k])
                 return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: slices out of order");
-        if (!(a->shrink >= 0.0f && a->shrink < 1.0f))
-            return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: shrink must be in [0, 1)");
+        if (!(a->shrink > -4.0f && a->shrink < 1.0f))
+            return fail(GBFSM_INVALID_ARG, "gbfsm_batch_plan: shrink must be in (-4, 1)");
     }
     return launch_batch_plan(*a, static_cast<cudaStream_t>(stream));
 }

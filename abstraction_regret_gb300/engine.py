@@ -212,7 +212,7 @@ class DevicePlan:
             # lane chunks fill at most one wave (32 per resident warp) unless even 1 MiB
             # chunks do not; slices scale lane chunks down by up to 1 - shrink; warp
             # chunks number fewer than 8 per resident persistent warp plus one per input
-            factor = 1.25 / (1.0 - self.shrink)
+            factor = 1.25 / (1.0 - max(self.shrink, 0.0))
             cap = int(factor * (LANE_GROUP * lw + int(total_bytes) // (1 << 20) + n)) + \
                 8 * pw + 2 * n + 64
         self.cap_dfa_chunks, self.cap_dfa_fixup = self.dfa_caps(engine, n, total_bytes)

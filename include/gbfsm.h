@@ -469,7 +469,8 @@ typedef struct gbfsm_batch_plan_args {
     int32_t n_slices;         /* 0 or 1: one lane range; else inputs cut into slices at
                                  slice_first (host values, ascending, slice_first[0] = 0,
                                  slice_first[n_slices] = n_inputs) */
-    float shrink;             /* lane chunks of slice k get the size x (1 - shrink k / n) */
+    float shrink;             /* lane chunks of slice k get the size x (1 - shrink k / n),
+                                 -4 < shrink < 1 (below 0: later slices get longer chunks) */
     int32_t slice_first[GBFSM_PLAN_MAX_SLICES + 1];
     int32_t cap_chunks;       /* capacities of the output arrays */
     int32_t cap_lane_tasks;
