@@ -16,7 +16,10 @@ inputs stay larger than L2 where the case's kernel streams them:
                      the c2 DFA (4096 states, no accepting state);
 * ``c5-live``        the serving loop over the c5 pool (16 NFAs, 16 DFAs): the first
                      2000 requests of the live trace, all arriving at once (the oracle
-                     checks 100 of them).
+                     checks 100 of them);
+* ``c3-warps``       the engine on the first 512 inputs of c3-sustained with lane chunks
+                     turned off, so that warp chunks in ``persistent_kernel`` do the work
+                     (the design the lane launch replaced).
 """
 
 from __future__ import annotations
@@ -33,7 +36,9 @@ def _check(name, got, want) -> None:
             raise SystemExit(f"{name}: {what} differ from the oracle")
 
 
-def run(case: str, steps: int) -> None:
+def run(case: str, steps: int) -> float | None:
+    """Run the case; returns the mean device time (ms) of its timed engine steps, when
+    it has any."""
     import torch
 
     from oracle import oracle as O
@@ -61,19 +66,25 @@ def run(case: str, steps: int) -> None:
                     if (int(f[i]), int(l[i])) != (int(want[0]), int(want[1])):
                         raise SystemExit(f"c5-live: request {i} differs from the oracle")
         return
-    if case in ("c1-live", "c4-sustained", "dfa-long"):
+    if case in ("c1-live", "c4-sustained", "dfa-long", "c3-warps"):
+        choices = None
         if case == "c1-live":
             b = W.c1("live")
         elif case == "c4-sustained":
             b = W.c4("sustained")
+        elif case == "c3-warps":
+            from .engine import NfaChoice
+
+            b = W.c3("sustained", n_inputs=512)
+            choices = [NfaChoice(lanes=False)]
         else:
             b = W.c2("sustained")
             n, length = 8, 2 << 20
             b = W.Batch("dfa-long", b.automata, np.zeros(n, np.int64),
                         W.uniform_bytes([1, 4], n * length),
                         W.offsets_of(np.full(n, length, dtype=np.int64)), {})
-        r = GraphRunner(PersistentEngine(b.automata, dev), b.aut_ids, b.data, b.offsets,
-                        with_examined=True)
+        r = GraphRunner(PersistentEngine(b.automata, dev, choices=choices), b.aut_ids, b.data,
+                        b.offsets, with_examined=True)
         with torch.cuda.stream(r.stream):
             r.replay()
         r.stream.synchronize()
@@ -89,11 +100,15 @@ def run(case: str, steps: int) -> None:
             for w, v in zip(want, res):
                 w[sel] = v
         _check(case, got, want)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(r.stream):
+            e0.record(r.stream)
             for _ in range(steps):
                 r.kernel_only(r.stream)
+            e1.record(r.stream)
         r.stream.synchronize()
-        return
+        return e0.elapsed_time(e1) / steps if steps else None
     if case == "c1-plain":
         b = W.c1("live")
         ex = CudaNFAExecutor(b.automata[0], "auto", dev)
@@ -119,11 +134,15 @@ def run(case: str, steps: int) -> None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("case", choices=["c1-live", "c1-plain", "c2-sustained", "c4-sustained",
-                                     "dfa-long", "c5-live"])
+                                     "dfa-long", "c5-live", "c3-warps"])
+    ap.add_argument("--time", action="store_true",
+                    help="also print the mean device time of the timed steps")
     ap.add_argument("--steps", type=int, default=2)
     args = ap.parse_args(argv)
-    run(args.case, args.steps)
+    ms = run(args.case, args.steps)
     print(f"{args.case}: verdicts equal to the oracle; {args.steps} more steps run")
+    if args.time and ms is not None:
+        print(f"{args.case}: {ms:.4f} ms per engine step (mean of {args.steps})")
     return 0
 
 
