@@ -45,6 +45,11 @@ from .staging import Results, Staging
 DFA_GROUP = 32
 NFA_BYTE_WEIGHT = 4  # task-ordering weight of an NFA byte relative to a DFA byte
 MIN_CHUNK = 256      # shortest speculative chunk (bytes)
+# shortest chunk of a pool whose NFAs all run in lanes with two-byte start sets of at
+# most one state on average: their chunk starts are cheap, so a small batch gains from
+# more, finer chunks (c1-live: 0.090 ms per step at 64 B against 0.151 ms at 256 B; a
+# c3 batch, whose starts often widen, is fastest at 192-256 B)
+MIN_CHUNK_SMALL_STARTS = 64
 LANE_GROUP = 32      # chunks per LANES task (one per lane)
 # an automaton's chunks run one per lane when its two-byte supersets are this small on
 # average: a lane starts from the superset when it has at most native.LANE_CAPACITY
@@ -291,7 +296,7 @@ class DevicePlan:
         a.lane_warps = eng.sm_count * eng.lane_warps_per_sm * self.lane_waves
         a.persist_warps = eng.resident_warps
         a.dfa_warps = eng.dfa_warps
-        a.min_chunk = MIN_CHUNK
+        a.min_chunk = eng.min_chunk
         a.fixed_chunk = eng.fixed_chunk
         if self.slices:
             a.n_slices = len(self.slices) - 1
@@ -525,6 +530,10 @@ class PersistentEngine:
             else:
                 cls.append(native.PLAN_NFA_WHOLE)
         self.aut_class = torch.tensor(cls, dtype=torch.int32, device=self.device)
+        nfa_ix = [i for i, k in enumerate(self.kinds) if k is Kind.NFA]
+        small_starts = bool(nfa_ix) and all(
+            bool(self.lane_ok[i]) and self.dev[i].pair_mean <= 1.0 for i in nfa_ix)
+        self.min_chunk = MIN_CHUNK_SMALL_STARTS if small_starts else MIN_CHUNK
         self.aut_dfa_chunk = (torch.tensor(self.dfa_chunk, dtype=torch.int32, device=self.device)
                               if any(self.dfa_chunk) else None)
         self.min_dfa_chunk = min([c for c in self.dfa_chunk if c] or [0])
@@ -536,7 +545,7 @@ class PersistentEngine:
                     lib.gbfsm_dfa_chunks_warps_per_sm(max(1, self.dfa_max_states)))
         self.fixed_chunk = -1 if chunk_bytes is None else max(0, int(chunk_bytes))
         if self.fixed_chunk > 0:
-            self.fixed_chunk = max(self.fixed_chunk, MIN_CHUNK)
+            self.fixed_chunk = max(self.fixed_chunk, self.min_chunk)
         self._dplan: DevicePlan | None = None
         self._h_aut = self._d_aut = None
 
@@ -544,24 +553,27 @@ class PersistentEngine:
 
     def auto_chunk_bytes(self, nfa_bytes: int) -> int:
         """Warp chunks: about four per resident warp of the persistent launch (a power of
-        two in [MIN_CHUNK, 1 MiB])."""
+        two in [the shortest chunk, 1 MiB])."""
         per = nfa_bytes // max(1, 4 * self.resident_warps)
-        size = max(MIN_CHUNK, 1 << max(0, int(per).bit_length() - 1))
+        size = max(getattr(self, "min_chunk", MIN_CHUNK),
+                   1 << max(0, int(per).bit_length() - 1))
         return int(min(size, 1 << 20))
 
     def auto_lane_chunk_bytes(self, lengths: np.ndarray, aut: np.ndarray) -> int:
-        """Lane chunks: the smallest size (a multiple of 64 bytes, at least MIN_CHUNK)
+        """Lane chunks: the smallest size (a multiple of 64 bytes, at least the shortest
+        chunk)
         whose LANES tasks (32 chunks each, per automaton) fit the lane launch's resident
         warps, so the batch runs in one full wave. A lane's steps are dependent L2 round
         trips: once every lane is busy, finer chunks only add per-chunk work, and a second
         partial wave adds its whole duration."""
         warps = self.sm_count * getattr(self, "lane_warps_per_sm", LANE_WARPS_PER_SM)
+        floor = getattr(self, "min_chunk", MIN_CHUNK)
         lengths = np.asarray(lengths, dtype=np.int64)
         aut = np.asarray(aut, dtype=np.int64)
         if lengths.size == 0:
-            return MIN_CHUNK
+            return floor
         total = int(lengths.sum())
-        size = max(MIN_CHUNK, -(-total // (warps * LANE_GROUP) // 64) * 64)
+        size = max(floor, -(-total // (warps * LANE_GROUP) // 64) * 64)
         order = np.argsort(aut, kind="stable")
         a_sorted, l_sorted = aut[order], lengths[order]
         seg = np.flatnonzero(np.r_[True, a_sorted[1:] != a_sorted[:-1]])
@@ -606,7 +618,8 @@ class PersistentEngine:
         chunk_w = chunk_l = 0
         if self.chunk_bytes is not None and nfa_idx.size:
             if self.chunk_bytes:
-                chunk_w = chunk_l = max(int(self.chunk_bytes), MIN_CHUNK)
+                chunk_w = chunk_l = max(int(self.chunk_bytes),
+                                        getattr(self, "min_chunk", MIN_CHUNK))
             else:
                 chunk_w = warp_chunk or self.auto_chunk_bytes(int(lengths[warp_in].sum()))
                 if isinstance(lane_chunk, np.ndarray):
@@ -617,7 +630,7 @@ class PersistentEngine:
             csize[warp_in] = chunk_w
             if isinstance(lane_chunk, np.ndarray) and not self.chunk_bytes:
                 csize[lane_in] = np.maximum(np.asarray(lane_chunk, np.int64)[lane_in],
-                                            MIN_CHUNK)
+                                            getattr(self, "min_chunk", MIN_CHUNK))
             else:
                 csize[lane_in] = chunk_l
         # every input of a lane automaton is chunked (a short one is a single exact
