@@ -22,11 +22,14 @@
 //      longest first, bucket by bucket;
 //   4. write the header: counts, chunk sizes, the lane task range of each slice, and a
 //      zeroed overflow counter.
-// plan_fill_kernel (grid, a warp per input): writes the chunk table (plus a sentinel
-//   chunk of index 0 after the last), the FIXUP, CHUNK and WHOLE tasks, the input ids of
-//   whole NFA inputs and DFA inputs, the LANES tasks (32 consecutive lane chunks each;
-//   every lane finds its own automaton) and the DFA groups (32 consecutive DFA inputs of
-//   the length-bucketed order; every lane finds its own DFA).
+// plan_fill_kernel (grid): a warp per input writes its FIXUP, DFA_FIXUP, CHUNK and WHOLE
+//   tasks, its warp chunks and its input id; a thread per chunk writes the lane chunks and
+//   the DFA chunks (with their tasks), finding its input by a binary search of the
+//   inputs' chunk prefix counts, so that one long input's thousands of chunks do not
+//   fall to one warp; then the sentinel chunk of index 0 after the last, the LANES tasks
+//   (32 consecutive lane chunks each; every lane finds its own automaton) and the DFA
+//   groups (32 consecutive DFA inputs of the length-bucketed order; every lane finds its
+//   own DFA).
 //
 // The reference has no counterpart: it launches one kernel per automaton and per call
 // with one thread or warp per whole input (src/gpufsm/backends/cuda/nfa.py:105-121).
@@ -48,6 +51,7 @@ struct PlanScratch {
     int32_t *first;     // first chunk of a split input; slot of a whole NFA input
     int32_t *fix;       // FIXUP task slot of a split input
     int32_t *lpre;      // lane chunks of the inputs before i (n + 1 entries)
+    int32_t *dpre;      // DFA chunks of the inputs before i (n + 1 entries)
     uint32_t *cursor;   // [kBuckets] WHOLE/CHUNK cursors, [kBuckets] DFA cursors
     int32_t *tbase;     // [kBuckets] first persistent slot of each work bucket
     int32_t *tdfa;      // [kBuckets] first persistent slot of each bucket's DFA groups
@@ -55,7 +59,7 @@ struct PlanScratch {
 };
 
 size_t scratch_bytes(int32_t n) {
-    return (size_t)4 * 4 * (size_t)n + 4 * ((size_t)n + 1) + 4 * (size_t)kBuckets * 2 +
+    return (size_t)4 * 4 * (size_t)n + 8 * ((size_t)n + 1) + 4 * (size_t)kBuckets * 2 +
            4 * (size_t)kBuckets * 2 + 4 * ((size_t)kBuckets + 1) + 256;
 }
 
@@ -67,7 +71,8 @@ PlanScratch carve(void *p, int32_t n) {
     s.first = w + 2 * (size_t)n;
     s.fix = w + 3 * (size_t)n;
     s.lpre = w + 4 * (size_t)n;
-    s.cursor = reinterpret_cast<uint32_t *>(s.lpre + n + 1);
+    s.dpre = s.lpre + n + 1;
+    s.cursor = reinterpret_cast<uint32_t *>(s.dpre + n + 1);
     s.tbase = reinterpret_cast<int32_t *>(s.cursor + 2 * kBuckets);
     s.tdfa = s.tbase + kBuckets;
     s.dbase = s.tdfa + kBuckets;
@@ -205,10 +210,14 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
             }
         }
     }
-    lane_bytes = block_sum(lane_bytes, red);
-    warp_bytes = block_sum(warp_bytes, red);
-    dfa_bytes = block_sum(dfa_bytes, red);
-    dfa_long = block_sum(dfa_long, red);
+    {  // the four totals in one block-wide pass
+        int64_t v4[4] = {lane_bytes, warp_bytes, dfa_bytes, dfa_long}, t4[4];
+        block_scan<4>(v4, t4, red);
+        lane_bytes = t4[0];
+        warp_bytes = t4[1];
+        dfa_bytes = t4[2];
+        dfa_long = t4[3];
+    }
     // the batch's DFA chunk length (before each DFA's minimum): rounding each input up to
     // whole chunks adds at most one chunk per input, so B / (warps - inputs) keeps the
     // chunks within one wave
@@ -319,6 +328,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
     for (int32_t i = lo; i < hi; ++i) {
         const int32_t c = s.cls[i];
         s.lpre[i] = (int32_t)ex[0];
+        s.dpre[i] = (int32_t)ex[4];
         const int32_t cnt = s.cnt[i];
         if (cnt > 0 && c == GBFSM_PLAN_DFA) {
             s.first[i] = (int32_t)(n_lane + n_warp + ex[4]);
@@ -340,7 +350,10 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
             ex[3] += 1;
         }
     }
-    if (threadIdx.x == kPlanThreads - 1) s.lpre[n] = (int32_t)n_lane;
+    if (threadIdx.x == kPlanThreads - 1) {
+        s.lpre[n] = (int32_t)n_lane;
+        s.dpre[n] = (int32_t)n_dfa_chunks;
+    }
     __syncthreads();
 
     // 4. bucket tables and the header (one warp)
@@ -404,6 +417,28 @@ __global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(gbfsm_batch_pla
     }
 }
 
+// Chunk k of cnt of input i (bytes [st, st + len)): even cuts.
+__device__ __forceinline__ gbfsm_chunk chunk_of(int32_t i, int32_t k, int32_t cnt, int64_t st,
+                                                int64_t len) {
+    gbfsm_chunk ch;
+    ch.input = i;
+    ch.index = k;
+    ch.begin = st + (int64_t)k * len / cnt;
+    ch.end = st + (int64_t)(k + 1) * len / cnt;
+    return ch;
+}
+
+// The last input i in [0, n) with pre[i] <= c (pre: non-decreasing prefix counts).
+__device__ __forceinline__ int32_t owner(const int32_t *pre, int32_t n, int32_t c) {
+    int32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int32_t mid = lo + (hi - lo + 1) / 2;
+        if (pre[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(256) plan_fill_kernel(gbfsm_batch_plan_args a, PlanScratch s) {
     const int32_t *h = a.header;
     if (h[GBFSM_PLAN_STATUS] != 0) return;
@@ -423,40 +458,24 @@ __global__ void __launch_bounds__(256) plan_fill_kernel(gbfsm_batch_plan_args a,
         const int64_t st = a.offsets[i];
         const int64_t len = input_len(a, i);
         const int32_t cnt = s.cnt[i];
-        if (cnt > 0 && c == GBFSM_PLAN_DFA) {  // a long DFA input: chunks walked by warps
-            const int32_t f = s.first[i];
-            const int32_t base = n_chunks - h[GBFSM_PLAN_DFA_CHUNKS];
-            for (int32_t k = (int32_t)lane; k < cnt; k += 32) {
-                gbfsm_chunk ch;
-                ch.input = i;
-                ch.index = k;
-                ch.begin = st + (int64_t)k * len / cnt;
-                ch.end = st + (int64_t)(k + 1) * len / cnt;
-                a.chunks[f + k] = ch;
-                a.tasks_dfa_chunk[f - base + k] =
-                    gbfsm_task{aut, f + k, 1, GBFSM_TASK_DFA_CHUNK};
-            }
+        if (cnt > 0 && c == GBFSM_PLAN_DFA) {  // a long DFA input (its chunks: below)
             if (lane == 0) {
-                a.tasks_dfa_fixup[s.fix[i]] = gbfsm_task{aut, f, cnt, GBFSM_TASK_DFA_FIXUP};
+                a.tasks_dfa_fixup[s.fix[i]] =
+                    gbfsm_task{aut, s.first[i], cnt, GBFSM_TASK_DFA_FIXUP};
                 if (a.dfa_latch) a.dfa_latch[i] = INT32_MAX;
             }
-        } else if (cnt > 0) {
+        } else if (cnt > 0 && c == GBFSM_PLAN_NFA_LANES) {  // lane chunks: below
+            if (lane == 0) tf[s.fix[i]] = gbfsm_task{aut, s.first[i], cnt, GBFSM_TASK_FIXUP};
+        } else if (cnt > 0) {  // warp chunks, each with its CHUNK task
             const int32_t f = s.first[i];
             int32_t slot0 = 0;
-            if (c != GBFSM_PLAN_NFA_LANES && lane == 0)
+            if (lane == 0)
                 slot0 = (int32_t)atomicAdd(&s.cursor[bucket_of(4 * (len / cnt))], (uint32_t)cnt);
             slot0 = __shfl_sync(GBFSM_FULL_MASK, slot0, 0);
+            const int b = bucket_of(4 * (len / cnt));
             for (int32_t k = (int32_t)lane; k < cnt; k += 32) {
-                gbfsm_chunk ch;
-                ch.input = i;
-                ch.index = k;
-                ch.begin = st + (int64_t)k * len / cnt;
-                ch.end = st + (int64_t)(k + 1) * len / cnt;
-                a.chunks[f + k] = ch;
-                if (c != GBFSM_PLAN_NFA_LANES) {
-                    const int b = bucket_of(4 * (len / cnt));
-                    tp[s.tbase[b] + slot0 + k] = gbfsm_task{aut, f + k, 1, GBFSM_TASK_CHUNK};
-                }
+                a.chunks[f + k] = chunk_of(i, k, cnt, st, len);
+                tp[s.tbase[b] + slot0 + k] = gbfsm_task{aut, f + k, 1, GBFSM_TASK_CHUNK};
             }
             if (lane == 0) tf[s.fix[i]] = gbfsm_task{aut, f, cnt, GBFSM_TASK_FIXUP};
         } else if (c == GBFSM_PLAN_NFA_WARP || c == GBFSM_PLAN_NFA_WHOLE) {
@@ -477,6 +496,23 @@ __global__ void __launch_bounds__(256) plan_fill_kernel(gbfsm_batch_plan_args a,
     }
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    // lane chunks: chunk c of the lane region belongs to the last input i with
+    // lpre[i] <= c (inputs without lane chunks share their successor's prefix)
+    for (int64_t c = tid; c < n_lane; c += nthreads) {
+        const int32_t i = owner(s.lpre, n, (int32_t)c);
+        const int32_t k = (int32_t)c - s.lpre[i];
+        a.chunks[c] = chunk_of(i, k, s.cnt[i], a.offsets[i], input_len(a, i));
+    }
+    // DFA chunks (after the lane and warp chunks), each with its DFA_CHUNK task
+    const int32_t n_dfa_chunks = h[GBFSM_PLAN_DFA_CHUNKS];
+    const int32_t dfa_base = n_chunks - n_dfa_chunks;
+    for (int64_t c = tid; c < n_dfa_chunks; c += nthreads) {
+        const int32_t i = owner(s.dpre, n, (int32_t)c);
+        const int32_t k = (int32_t)c - s.dpre[i];
+        const int32_t aut = a.aut_ids ? a.aut_ids[i] : 0;
+        a.chunks[dfa_base + c] = chunk_of(i, k, s.cnt[i], a.offsets[i], input_len(a, i));
+        a.tasks_dfa_chunk[c] = gbfsm_task{aut, dfa_base + (int32_t)c, 1, GBFSM_TASK_DFA_CHUNK};
+    }
     if (tid == 0 && n_chunks < a.cap_chunks) {  // sentinel: no next chunk of the same input
         gbfsm_chunk z;
         z.input = -1;
