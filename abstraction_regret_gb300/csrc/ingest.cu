@@ -5,12 +5,16 @@
 //
 // On a device that reads pageable host memory coherently (GB300 with NVLink-C2C: address
 // translation through the host's page tables), the source buffers need no registration:
-// the copy kernel loads them directly. One warp copies one input: each lane writes whole
-// 16-byte blocks of the destination, each made of two aligned 16-byte source loads joined
-// by shifts (the source and destination need not share an alignment);
-// the partial blocks at the two ends of an input are written byte by byte. A load never
-// touches an aligned 16-byte block that holds no byte of its input, so it never touches a
-// page the input does not.
+// the copy kernel loads them directly. The destination is cut into 8 KiB windows, taken by
+// the warps of the grid in turn, so that a long input is copied by many warps and a batch
+// of unequal inputs keeps every warp busy to the end (one warp per input left a 1 MiB
+// input to one warp). In a window, the inputs that overlap it are taken 32 at a time:
+// pieces under 64 bytes are copied byte by byte by one lane each, longer ones by the whole
+// warp, each lane writing whole 16-byte blocks of the destination made of two aligned
+// 16-byte source loads joined by shifts (the source and destination need not share an
+// alignment), and the partial blocks at the two ends of a piece byte by byte. Every
+// destination byte is written once. A load never touches an aligned 16-byte block that
+// holds no byte of its input, so it never touches a page the input does not.
 //
 // The reference packs every batch on the host and copies it synchronously from pageable
 // memory, widened to int32 (src/gpufsm/core/packing.py:35-63,
@@ -44,23 +48,83 @@ __device__ __forceinline__ uint4 ld16_unaligned(const uint8_t *p) {
     return make_uint4((uint32_t)o0, (uint32_t)(o0 >> 32), (uint32_t)o1, (uint32_t)(o1 >> 32));
 }
 
-__global__ void __launch_bounds__(256) gather_inputs_kernel(const uint64_t *__restrict__ src,
-                                                            const int64_t *__restrict__ offsets,
-                                                            int32_t n, uint8_t *__restrict__ dst) {
+constexpr int64_t kGatherWindow = 8192;  // destination bytes per warp task
+constexpr int64_t kGatherSmall = 64;     // pieces shorter than this: one lane each
+#ifndef GBFSM_GATHER_THREADS
+#define GBFSM_GATHER_THREADS 256
+#endif
+#ifndef GBFSM_GATHER_CTAS_PER_SM
+#define GBFSM_GATHER_CTAS_PER_SM 2  // the host link saturates at 2 CTAs of 256 per SM
+#endif
+constexpr int kGatherThreads = GBFSM_GATHER_THREADS;
+constexpr int kGatherCtasPerSm = GBFSM_GATHER_CTAS_PER_SM;
+
+// The warp copies dst[lo, hi) from s (s holds the byte of dst[lo]).
+__device__ __forceinline__ void copy_piece(const uint8_t *s, uint8_t *__restrict__ dst,
+                                           int64_t lo, int64_t hi, uint32_t lane) {
+    const int64_t a = (lo + 15) & ~(int64_t)15, z = hi & ~(int64_t)15;
+    if (a >= z) {  // no whole block: fewer than 32 bytes
+        const int64_t k = lo + lane;
+        if (k < hi) dst[k] = s[k - lo];
+        return;
+    }
+    if (lo + lane < a) dst[lo + lane] = s[lane];                  // head, under 16 bytes
+    if (z + lane < hi) dst[z + lane] = s[z + lane - lo];          // tail, under 16 bytes
+    for (int64_t b = a + 16 * (int64_t)lane; b < z; b += 16 * 32 * 4) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (b + 512 * u < z) v[u] = ld16_unaligned(s + (b + 512 * u - lo));
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (b + 512 * u < z) *reinterpret_cast<uint4 *>(dst + b + 512 * u) = v[u];
+    }
+}
+
+__global__ void __launch_bounds__(kGatherThreads) gather_inputs_kernel(
+    const uint64_t *__restrict__ src, const int64_t *__restrict__ offsets, int32_t n,
+    uint8_t *__restrict__ dst) {
     const uint32_t lane = lane_id();
+    const int64_t first = offsets[0], last = offsets[n];
+    if (last <= first) return;
+    const int64_t w0 = first & ~(int64_t)15;  // windows start on 16-byte blocks
+    const int64_t windows = (last - w0 + kGatherWindow - 1) / kGatherWindow;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
-        const uint8_t *s = reinterpret_cast<const uint8_t *>(src[i]);
-        const int64_t d0 = offsets[i], d1 = offsets[i + 1];
-        if (d1 <= d0) continue;
-        const int64_t b0 = d0 & ~(int64_t)15, b1 = (d1 + 15) & ~(int64_t)15;
-        for (int64_t b = b0 + 16 * (int64_t)lane; b < b1; b += 16 * 32) {
-            const int64_t lo = b > d0 ? b : d0, hi = b + 16 < d1 ? b + 16 : d1;
-            if (lo == b && hi == b + 16) {
-                *reinterpret_cast<uint4 *>(dst + b) = ld16_unaligned(s + (b - d0));
-            } else {
-                for (int64_t k = lo; k < hi; ++k) dst[k] = s[k - d0];
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < windows;
+         w += nwarps) {
+        const int64_t wl = w0 + w * kGatherWindow;
+        const int64_t wh = wl + kGatherWindow < last ? wl + kGatherWindow : last;
+        // the first input that ends after wl (input n - 1 does: wl < last)
+        int32_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (offsets[mid + 1] > wl) hi = mid;
+            else lo = mid + 1;
+        }
+        for (int32_t g = lo; g < n; g += 32) {
+            const int32_t i = g + (int32_t)lane;
+            int64_t d0 = wh, d1 = wh;
+            if (i < n) {
+                d0 = offsets[i];
+                d1 = offsets[i + 1];
             }
+            const bool past = d0 >= wh;  // this input and every later one start after the window
+            const int64_t a = d0 > wl ? d0 : wl, b = d1 < wh ? d1 : wh;
+            const bool live = !past && a < b;
+            const uint8_t *s = live ? reinterpret_cast<const uint8_t *>(src[i]) + (a - d0) : nullptr;
+            if (live && b - a < kGatherSmall)
+                for (int64_t k = a; k < b; ++k) dst[k] = s[k - a];
+            uint32_t big = __ballot_sync(0xffffffffu, live && b - a >= kGatherSmall);
+            while (big) {
+                const int j = __ffs(big) - 1;
+                big &= big - 1;
+                const int64_t aj = __shfl_sync(0xffffffffu, a, j);
+                const int64_t bj = __shfl_sync(0xffffffffu, b, j);
+                const uint8_t *sj = reinterpret_cast<const uint8_t *>(
+                    __shfl_sync(0xffffffffu, reinterpret_cast<uint64_t>(s), j));
+                copy_piece(sj, dst, aj, bj, lane);
+            }
+            if (__any_sync(0xffffffffu, past)) break;
         }
     }
 }
@@ -70,10 +134,8 @@ __global__ void __launch_bounds__(256) gather_inputs_kernel(const uint64_t *__re
 gbfsm_status launch_gather_inputs(const uint64_t *src, const int64_t *offsets, int32_t n,
                                   uint8_t *dst, cudaStream_t stream) {
     if (n <= 0) return GBFSM_OK;
-    int grid = (n + 7) / 8;  // 8 warps per CTA, a warp per input
-    const int cap = sm_count() * 8;
-    if (grid > cap) grid = cap;
-    gather_inputs_kernel<<<grid, 256, 0, stream>>>(src, offsets, n, dst);
+    gather_inputs_kernel<<<sm_count() * kGatherCtasPerSm, kGatherThreads, 0, stream>>>(
+        src, offsets, n, dst);
     GBFSM_LAUNCH_CHECK("gather_inputs_kernel launch");
     return GBFSM_OK;
 }

@@ -74,6 +74,12 @@ DFA_CHUNK_PER_STATE = 8
 # shortest chunk; 1 or more: no limit but the next chunk's end (the walk stops at that
 # chunk's collapse, or covers it whole when it never collapses)
 DFA_OVERLAP_CHUNKS = 1.0
+# a host batch the device gathers in place (staging.py) of at least PIPELINE_MIN_BYTES is
+# gathered in PIPELINE_PARTS slices of contiguous inputs, each slice's lane tasks starting
+# as soon as its bytes are in (run_requests); PIPELINE_LANE_WAVES as in GraphRunner
+PIPELINE_PARTS = 8
+PIPELINE_MIN_BYTES = 32 << 20
+PIPELINE_LANE_WAVES = 2
 
 
 def dfa_chunk_length(num_states: int) -> int:
@@ -272,13 +278,20 @@ class DevicePlan:
     def _hdr(self, word: int) -> int:
         return self.header.data_ptr() + 4 * word
 
-    def plan(self, d_off, d_ends, d_aut, stream, n_inputs: int | None = None) -> None:
+    def plan(self, d_off, d_ends, d_aut, stream, n_inputs: int | None = None,
+             slices=None) -> None:
         """Enqueue planning for the inputs at ``d_off`` (``d_ends``, ``d_aut``: device
-        tensors or None)."""
+        tensors or None). ``slices``: this batch's slice starts (plus ``n_inputs``), in
+        place of the ones the plan was built with."""
         eng = self.engine
         n = self.n if n_inputs is None else int(n_inputs)
         if n > self.n:
             raise ValueError(f"{n} inputs above the plan's capacity of {self.n}")
+        if slices is not None:
+            slices = list(slices)
+            if not 2 < len(slices) <= native.PLAN_MAX_SLICES + 1:
+                raise ValueError(f"2 to {native.PLAN_MAX_SLICES} slices")
+            self.slices = slices
         a = native.BatchPlanArgs()
         a.n_inputs = n
         a.n_automata = len(eng.automata)
@@ -547,6 +560,11 @@ class PersistentEngine:
         if self.fixed_chunk > 0:
             self.fixed_chunk = max(self.fixed_chunk, self.min_chunk)
         self._dplan: DevicePlan | None = None
+        self._pplan: DevicePlan | None = None  # pipelined host batches (run_requests)
+        self._copy_stream = None
+        self._slice_streams: list = []
+        self.pipeline_parts = PIPELINE_PARTS  # 0 or 1: gather a host batch whole first
+        self.last_slices = 0  # slices of the last run_requests batch (0: not pipelined)
         self._h_aut = self._d_aut = None
 
     # ---- task queue ---------------------------------------------------------------------
@@ -816,16 +834,51 @@ class PersistentEngine:
             launches += 1
         return launches
 
-    def device_plan(self, n_inputs: int, total_bytes: int) -> DevicePlan:
-        """Plan buffers for a batch of this size (kept and reused while batches fit)."""
-        p = self._dplan
+    def device_plan(self, n_inputs: int, total_bytes: int, pipelined: bool = False) -> DevicePlan:
+        """Plan buffers for a batch of this size (kept and reused while batches fit);
+        ``pipelined``: the plan of sliced host batches (its slices given per batch)."""
+        p = self._pplan if pipelined else self._dplan
         if p is None or p.n < n_inputs or p.total_bytes < total_bytes:
             n = max(int(n_inputs), 2 * (p.n if p else 0), 64)
             total = max(int(total_bytes), 2 * (p.total_bytes if p else 0), 1 << 20)
-            self._dplan = None  # free the old buffers first
-            p = DevicePlan(self, n, total)
-            self._dplan = p
+            if pipelined:
+                self._pplan = None  # free the old buffers first
+                p = DevicePlan(self, n, total, slices=[0, 1, 2], lane_waves=PIPELINE_LANE_WAVES)
+                self._pplan = p
+            else:
+                self._dplan = None
+                p = DevicePlan(self, n, total)
+                self._dplan = p
         return p
+
+    def _pipelined_launch(self, n: int, h_off: np.ndarray, total: int, d_data, d_off, d_aut,
+                          res, with_examined: bool, stream) -> DevicePlan | None:
+        """Gather a deferred host batch in slices on a copy stream, each slice's lane tasks
+        on a stream of its own once its bytes are in, the rest of the step on ``stream``;
+        None (nothing enqueued) when the batch makes fewer than two slices."""
+        spans = slice_bounds(h_off, min(self.pipeline_parts, native.PLAN_MAX_SLICES))
+        if len(spans) < 2:
+            return None
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream(self.device)
+            self._slice_streams = [torch.cuda.Stream(self.device)
+                                   for _ in range(native.PLAN_MAX_SLICES)]
+        plan = self.device_plan(n, total, pipelined=True)
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        self._copy_stream.wait_event(fork)
+        ready = []
+        for a, b in spans:
+            self._staging.gather_range(a, b, self._copy_stream)
+            ev = torch.cuda.Event()
+            ev.record(self._copy_stream)
+            ready.append(ev)
+        plan.plan(d_off, None, d_aut, stream, n, slices=[a for a, _ in spans] + [n])
+        plan.launch(d_data.data_ptr(), d_off, None, res.d[0], res.d[1],
+                    res.d[2] if with_examined else None, stream,
+                    lane_slices=list(zip(self._slice_streams, ready)))
+        self.last_slices = len(spans)
+        return plan
 
     def upload_aut_ids(self, aut_ids, stream):
         """Device int32 copy of the batch's automaton ids (None for a one-automaton pool,
@@ -850,19 +903,30 @@ class PersistentEngine:
         on the device.
 
         Returns ``(flags, lens, examined | None, kernel_ms, transfer_ms)`` as numpy arrays
-        indexed like ``inputs``; ``kernel_ms`` covers the planning and simulation launches.
+        indexed like ``inputs``; ``kernel_ms`` covers the planning and simulation launches
+        (and, for a batch the device gathers in slices, the gather they overlap).
+        A batch the device gathers in place, of at least PIPELINE_MIN_BYTES, is gathered
+        in ``pipeline_parts`` slices, each slice's lane tasks running as its bytes arrive.
         """
         t0 = time.perf_counter()
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
         d_aut = self.upload_aut_ids(aut_ids, stream)
-        d_data, d_off, _, total = self._staging.put(inputs, stream)
+        d_data, d_off, h_off, total = self._staging.put(inputs, stream,
+                                                        defer=self.pipeline_parts > 1)
         self._results.ensure(max(n, 1))
         res = self._results
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        if n:
+        plan = None
+        self.last_slices = 0
+        if self._staging.deferred and n > 1 and total >= PIPELINE_MIN_BYTES:
+            plan = self._pipelined_launch(n, h_off, total, d_data, d_off, d_aut, res,
+                                          with_examined, stream)
+        if plan is None and n:
+            if self._staging.deferred:
+                self._staging.gather_range(0, n, stream)
             plan = self.device_plan(n, total)
             plan.plan(d_off, None, d_aut, stream, n)
             plan.launch(d_data.data_ptr(), d_off, None, res.d[0], res.d[1],

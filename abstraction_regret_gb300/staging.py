@@ -88,6 +88,7 @@ class Staging:
         self.gather = gather
         self._pageable = None
         self.last_path = None
+        self.deferred = False  # the last put left its gather to the caller
 
     def _can_gather(self) -> bool:
         if self._pageable is None:
@@ -112,12 +113,16 @@ class Staging:
             self._h_ptr = torch.empty(self._cap_off, dtype=torch.int64, pin_memory=True)
             self._d_ptr = torch.empty(self._cap_off, dtype=torch.int64, device=self.device)
 
-    def put(self, inputs, stream: torch.cuda.Stream):
+    def put(self, inputs, stream: torch.cuda.Stream, defer: bool = False):
         """Pack ``inputs`` (bytes-like objects) and start their copy on ``stream``.
 
         Returns ``(d_data, d_offsets, h_offsets, total_bytes)``; device tensors are views
-        of the staging buffers (valid until the next ``put``).
+        of the staging buffers (valid until the next ``put``). ``defer``: when the batch
+        is gathered in place, enqueue only its address and offset tables and set
+        ``deferred``; the caller then runs ``gather_range`` over every input (in ranges, on
+        streams that follow ``stream``).
         """
+        self.deferred = False
         n = len(inputs)
         lens = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
         total = int(lens.sum()) if n else 0
@@ -131,17 +136,15 @@ class Staging:
             # the GPU reads each input where it lies; the caller keeps ``inputs`` alive
             # until the stream has passed this copy (the executors synchronise first)
             addresses(inputs, self._h_ptr.numpy())
-            from . import native
-
             with torch.cuda.stream(stream):
                 self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
                 self._d_ptr[:n].copy_(self._h_ptr[:n], non_blocking=True)
                 if padded > total:
                     self._d_data[total:padded].zero_()
-                native.check(native.lib().gbfsm_gather_inputs(
-                    self._d_ptr.data_ptr(), self._d_off.data_ptr(), n,
-                    self._d_data.data_ptr(), stream.cuda_stream), "gbfsm_gather_inputs")
             self.last_path = "gather"
+            self.deferred = defer
+            if not defer:
+                self.gather_range(0, n, stream)
             return self._d_data[:padded], self._d_off[: n + 1], h_off, total
         self.last_path = "pack"
         h_data = self._h_data.numpy()
@@ -156,6 +159,18 @@ class Staging:
             self._d_data[:padded].copy_(self._h_data[:padded], non_blocking=True)
             self._d_off[: n + 1].copy_(self._h_off[: n + 1], non_blocking=True)
         return self._d_data[:padded], self._d_off[: n + 1], h_off, total
+
+
+    def gather_range(self, first: int, last: int, stream: torch.cuda.Stream) -> None:
+        """Enqueue on ``stream`` the copy of inputs [first, last) of the last ``put`` (a
+        gathered batch) into their places in the device buffer."""
+        from . import native
+
+        if last <= first:
+            return
+        native.check(native.lib().gbfsm_gather_inputs(
+            self._d_ptr.data_ptr() + 8 * first, self._d_off.data_ptr() + 8 * first,
+            last - first, self._d_data.data_ptr(), stream.cuda_stream), "gbfsm_gather_inputs")
 
 
 class Results:

@@ -686,13 +686,17 @@ def run_batch_section(batch, flags, lens, steps: int = 3) -> dict:
     ex = make_nfa_executor(nfa, "auto")
     ingest = None
     if ex.last_path == "engine":
-        ingest = ex.engine().engine._staging.last_path
+        eng = ex.engine().engine
+        ingest = eng._staging.last_path
+        if eng.last_slices:
+            ingest += f" in {eng.last_slices} slices, each slice's lanes starting on arrival"
     return {"value": batch.total_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "ms": ms,
             "calls": steps, "path": ex.last_path, "ingest": ingest,
             "kernel_ms": float(np.median(kern)),
             "note": "wall clock per call (median), host bytes in, verdicts out; kernel_ms: "
-                    "planning and simulation launches (the rest is ingest, verdicts and "
-                    "host work)"}
+                    "planning and simulation launches, with the gather they overlap when "
+                    "the batch is gathered in slices (the rest is host work, the address "
+                    "and offset tables, verdicts)"}
 
 
 def reference_gpu_section(dev, steps: int) -> dict:

@@ -367,7 +367,10 @@ int32_t gbfsm_pageable_access(void);
  * arrays; dst is device memory of at least offsets[n_inputs] rounded up to 16 bytes. A
  * source may be device memory, page-locked host memory mapped into the device, or, where
  * gbfsm_pageable_access() > 0, any pageable host memory; it is read in aligned 16-byte
- * blocks that each hold at least one of its bytes. One warp per input; stream-ordered.
+ * blocks that each hold at least one of its bytes. offsets must not decrease; the copy
+ * covers dst[offsets[0] .. offsets[n_inputs]), so a contiguous range of a batch's inputs
+ * (src_ptrs + k, offsets + k) is gathered alone, every byte written once (ranges may be
+ * gathered concurrently). Warps take 8 KiB windows of the destination; stream-ordered.
  * No counterpart in the reference (which packs and copies every batch on the host). */
 gbfsm_status gbfsm_gather_inputs(const uint64_t *src_ptrs, const int64_t *offsets,
                                  int32_t n_inputs, uint8_t *dst, void *stream);
