@@ -898,7 +898,7 @@ class PersistentEngine:
             self._d_aut[:n].copy_(self._h_aut[:n], non_blocking=True)
         return self._d_aut
 
-    def run_requests(self, aut_ids, inputs, with_examined: bool = False):
+    def run_requests(self, aut_ids, inputs, with_examined: bool = False, lengths=None):
         """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``; the batch is planned
         on the device.
 
@@ -907,13 +907,15 @@ class PersistentEngine:
         (and, for a batch the device gathers in slices, the gather they overlap).
         A batch the device gathers in place, of at least PIPELINE_MIN_BYTES, is gathered
         in ``pipeline_parts`` slices, each slice's lane tasks running as its bytes arrive.
+        ``lengths``: the inputs' lengths (int64), when the caller has them already.
         """
         t0 = time.perf_counter()
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
         d_aut = self.upload_aut_ids(aut_ids, stream)
         d_data, d_off, h_off, total = self._staging.put(inputs, stream,
-                                                        defer=self.pipeline_parts > 1)
+                                                        defer=self.pipeline_parts > 1,
+                                                        lengths=lengths)
         self._results.ensure(max(n, 1))
         res = self._results
         e0 = torch.cuda.Event(enable_timing=True)

@@ -70,10 +70,12 @@ NFA_TECHNIQUES: dict[str, tuple[int, int, bool]] = {
 MAX_INPUT_BYTES = (1 << 31) - 1  # match_len is int32, as in the reference
 
 
-def _check_inputs(inputs) -> None:
-    for b in inputs:
-        if len(b) > MAX_INPUT_BYTES:
-            raise ValueError(f"an input of {len(b)} bytes exceeds the int32 match_len range")
+def _lengths(inputs) -> np.ndarray:
+    """The inputs' lengths (int64); raises when one exceeds the int32 match_len range."""
+    lens = np.fromiter(map(len, inputs), dtype=np.int64, count=len(inputs))
+    if lens.size and int(lens.max()) > MAX_INPUT_BYTES:
+        raise ValueError(f"an input of {int(lens.max())} bytes exceeds the int32 match_len range")
+    return lens
 
 
 class _BatchExecutor:
@@ -89,9 +91,10 @@ class _BatchExecutor:
     def _launch(self, d_data, d_off, n, d_flags, d_lens, d_examined, stream) -> None:
         raise NotImplementedError
 
-    def run_arrays(self, inputs, with_examined: bool = False):
+    def run_arrays(self, inputs, with_examined: bool = False, lengths=None):
         """``(flags, lens, examined | None, kernel_ms, transfer_ms)`` for a batch."""
-        _check_inputs(inputs)
+        if lengths is None:
+            lengths = _lengths(inputs)
         t0 = time.perf_counter()
         n = len(inputs)
         stream = torch.cuda.current_stream(self.device)
@@ -99,7 +102,7 @@ class _BatchExecutor:
         e1 = torch.cuda.Event(enable_timing=True)
         if self.end_to_end:
             e0.record(stream)
-        d_data, d_off, _, _ = self._staging.put(inputs, stream)
+        d_data, d_off, _, _ = self._staging.put(inputs, stream, lengths=lengths)
         self._results.ensure(max(n, 1))
         r = self._results
         if not self.end_to_end:
@@ -209,10 +212,11 @@ class CudaPersistentExecutor:
         self.engine = PersistentEngine([automaton], device, choices=[choice],
                                        resident=[resident] if resident is not None else None)
 
-    def run_arrays(self, inputs, with_examined: bool = False):
-        _check_inputs(inputs)
+    def run_arrays(self, inputs, with_examined: bool = False, lengths=None):
+        if lengths is None:
+            lengths = _lengths(inputs)
         return self.engine.run_requests(np.zeros(len(inputs), dtype=np.int64), inputs,
-                                        with_examined)
+                                        with_examined, lengths=lengths)
 
     def run_batch(self, inputs) -> list[Result]:
         if not inputs:
@@ -248,13 +252,12 @@ class CudaAutoNFAExecutor:
         return self._engine
 
     def run_arrays(self, inputs, with_examined: bool = False):
-        _check_inputs(inputs)
-        lengths = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=len(inputs))
+        lengths = _lengths(inputs)
         if prefer_engine(self.plain.dev, lengths):
             self.last_path = "engine"
-            return self.engine().run_arrays(inputs, with_examined)
+            return self.engine().run_arrays(inputs, with_examined, lengths)
         self.last_path = "plain"
-        return self.plain.run_arrays(inputs, with_examined)
+        return self.plain.run_arrays(inputs, with_examined, lengths)
 
     def run_batch(self, inputs) -> list[Result]:
         if not inputs:

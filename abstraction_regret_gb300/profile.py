@@ -19,7 +19,11 @@ inputs stay larger than L2 where the case's kernel streams them:
                      checks 100 of them);
 * ``c3-warps``       the engine on the first 512 inputs of c3-sustained with lane chunks
                      turned off, so that warp chunks in ``persistent_kernel`` do the work
-                     (the design the lane launch replaced).
+                     (the design the lane launch replaced);
+* ``gather``         the batch gather (``gather_inputs_kernel``) of the first 1024
+                     c3-sustained inputs as Python ``bytes`` (130 MB, read in place from
+                     pageable host memory); the device buffer is checked byte for byte
+                     against the packed batch instead of the oracle.
 """
 
 from __future__ import annotations
@@ -48,6 +52,25 @@ def run(case: str, steps: int) -> float | None:
     from .executors import CudaDFAExecutor, CudaNFAExecutor
 
     dev = torch.device("cuda", torch.cuda.current_device())
+    if case == "gather":
+        from .staging import Staging
+
+        b = W.c3("sustained").subset(np.arange(1024))
+        inputs = b.inputs()
+        st = Staging(dev, gather=True)
+        stream = torch.cuda.current_stream(dev)
+        d_data, _, _, total = st.put(inputs, stream)
+        stream.synchronize()
+        if not np.array_equal(d_data[:total].cpu().numpy(), b.data[:total]):
+            raise SystemExit("gather: the device buffer differs from the packed batch")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            st.put(inputs, stream)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / steps if steps else None
     if case == "c5-live":
         from .serving import Server
 
@@ -134,13 +157,15 @@ def run(case: str, steps: int) -> float | None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("case", choices=["c1-live", "c1-plain", "c2-sustained", "c4-sustained",
-                                     "dfa-long", "c5-live", "c3-warps"])
+                                     "dfa-long", "c5-live", "c3-warps", "gather"])
     ap.add_argument("--time", action="store_true",
                     help="also print the mean device time of the timed steps")
     ap.add_argument("--steps", type=int, default=2)
     args = ap.parse_args(argv)
     ms = run(args.case, args.steps)
-    print(f"{args.case}: verdicts equal to the oracle; {args.steps} more steps run")
+    checked = "device buffer equal to the packed batch" if args.case == "gather" else \
+        "verdicts equal to the oracle"
+    print(f"{args.case}: {checked}; {args.steps} more steps run")
     if args.time and ms is not None:
         print(f"{args.case}: {ms:.4f} ms per engine step (mean of {args.steps})")
     return 0

@@ -37,11 +37,11 @@ def batch_results(
     transfer_ms: float = 0.0,
 ) -> list[Result]:
     """One :class:`Result` per input, with the batch's times on the first one only."""
-    f = flags.tolist() if hasattr(flags, "tolist") else [bool(x) for x in flags]
+    # verdicts as plain Python bools and ints, converted in bulk, then positional
+    # construction: about half the time of per-item conversion and keyword construction
+    f = (flags != 0).tolist() if hasattr(flags, "tolist") else [bool(x) for x in flags]
     m = lens.tolist() if hasattr(lens, "tolist") else [int(x) for x in lens]
-    # positional construction of plain Python values: about half the time of keyword
-    # construction for large batches
-    out = [Result(a != 0, b) for a, b in zip(f, m)]
+    out = [Result(a, b) for a, b in zip(f, m)]
     if out:
         first = out[0]
         first.kernel_ms = kernel_ms

@@ -55,7 +55,7 @@ def addresses(inputs, out: np.ndarray) -> None:
     ``bytes`` takes the addresses from ``id()`` at once (a few microseconds per thousand
     inputs instead of one ``ctypes`` call each)."""
     n = len(inputs)
-    if _BYTES_OFFSET is not None and all(type(b) is bytes for b in inputs):
+    if _BYTES_OFFSET is not None and set(map(type, inputs)) == {bytes}:
         out[:n] = np.fromiter(map(id, inputs), dtype=np.int64, count=n)
         out[:n] += _BYTES_OFFSET
         return
@@ -113,18 +113,20 @@ class Staging:
             self._h_ptr = torch.empty(self._cap_off, dtype=torch.int64, pin_memory=True)
             self._d_ptr = torch.empty(self._cap_off, dtype=torch.int64, device=self.device)
 
-    def put(self, inputs, stream: torch.cuda.Stream, defer: bool = False):
+    def put(self, inputs, stream: torch.cuda.Stream, defer: bool = False, lengths=None):
         """Pack ``inputs`` (bytes-like objects) and start their copy on ``stream``.
 
         Returns ``(d_data, d_offsets, h_offsets, total_bytes)``; device tensors are views
         of the staging buffers (valid until the next ``put``). ``defer``: when the batch
         is gathered in place, enqueue only its address and offset tables and set
         ``deferred``; the caller then runs ``gather_range`` over every input (in ranges, on
-        streams that follow ``stream``).
+        streams that follow ``stream``). ``lengths``: the inputs' lengths (int64), when
+        the caller has them already.
         """
         self.deferred = False
         n = len(inputs)
-        lens = np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
+        lens = lengths if lengths is not None else \
+            np.fromiter((len(b) for b in inputs), dtype=np.int64, count=n)
         total = int(lens.sum()) if n else 0
         padded = max(PAD, -(-total // PAD) * PAD)
         self._ensure(padded, n + 1)
