@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(kGatherThreads) gather_inputs_kernel(
             if (offsets[mid + 1] > wl) hi = mid;
             else lo = mid + 1;
         }
-        for (int32_t g = lo; g < n; g += 32) {
-            const int32_t i = g + (int32_t)lane;
+        for (int64_t g = lo; g < n; g += 32) {
+            const int64_t i = g + (int64_t)lane;
             int64_t d0 = wh, d1 = wh;
             if (i < n) {
                 d0 = offsets[i];
