@@ -39,7 +39,7 @@ import torch
 from . import native
 from .device import DeviceDFA, DeviceNFA, resolve_device
 from .registry import Kind
-from .result import Result, batch_results
+from .result import Result, blank_results, fill_results
 from .staging import Results, Staging
 
 DFA_GROUP = 32
@@ -901,7 +901,8 @@ class PersistentEngine:
             self._d_aut[:n].copy_(self._h_aut[:n], non_blocking=True)
         return self._d_aut
 
-    def run_requests(self, aut_ids, inputs, with_examined: bool = False, lengths=None):
+    def run_requests(self, aut_ids, inputs, with_examined: bool = False, lengths=None,
+                     idle=None):
         """Host path: ``inputs[i]`` runs on automaton ``aut_ids[i]``; the batch is planned
         on the device.
 
@@ -911,6 +912,7 @@ class PersistentEngine:
         A batch the device gathers in place, of at least PIPELINE_MIN_BYTES, is gathered
         in ``pipeline_parts`` slices, each slice's lane tasks running as its bytes arrive.
         ``lengths``: the inputs' lengths (int64), when the caller has them already.
+        ``idle``: called once every launch is enqueued, before the host waits for them.
         """
         t0 = time.perf_counter()
         n = len(inputs)
@@ -940,6 +942,8 @@ class PersistentEngine:
         res.fetch(n, stream)
         if n:
             plan.fetch_header(stream)
+        if idle is not None:
+            idle()
         stream.synchronize()
         if n:
             plan.check()
@@ -959,8 +963,10 @@ class PersistentEngine:
             return []
         aut = [r[0] for r in requests]
         data = [r[1] for r in requests]
-        flags, lens, _, kms, tms = self.run_requests(aut, data)
-        return batch_results(flags, lens, kms, tms)
+        out: list = []
+        flags, lens, _, kms, tms = self.run_requests(
+            aut, data, idle=lambda: out.extend(blank_results(len(data))))
+        return fill_results(out, flags, lens, kms, tms)
 
 
 def slice_bounds(offsets: np.ndarray, parts: int) -> list[tuple[int, int]]:

@@ -2,8 +2,10 @@
 
 An executor owns one automaton resident on the device and runs batches of inputs
 through one technique. ``run(bytes)`` is ``run_batch([bytes])[0]``; ``run_batch`` makes
-one launch for the whole batch and reports through ``batch_results`` (the batch's kernel
-time on result 0, reference core/result.py:27-50).
+one launch for the whole batch and reports with the convention of ``batch_results`` (the
+batch's kernel time on result 0, reference core/result.py:27-50): its ``Result`` objects
+are built while the device runs (``blank_results``) and given their verdicts once it has
+finished (``fill_results``).
 
 Technique names. The reference's CUDA names are registered with the meaning they have
 there (src/gpufsm/backends/cuda/nfa.py:26-41, dfa.py:50-53), so callers and the
@@ -47,7 +49,7 @@ from .autotune import choose_nfa_plan, prefer_engine
 from .device import DeviceDFA, DeviceNFA, resolve_device
 from .engine import NfaChoice, PersistentEngine
 from .registry import Backend, Kind, register, register_availability, set_unavailable_reason
-from .result import Result, batch_results
+from .result import Result, blank_results, fill_results
 from .staging import Results, Staging
 
 # technique -> (engine technique, stage edge rows, end-to-end timing)
@@ -91,8 +93,9 @@ class _BatchExecutor:
     def _launch(self, d_data, d_off, n, d_flags, d_lens, d_examined, stream) -> None:
         raise NotImplementedError
 
-    def run_arrays(self, inputs, with_examined: bool = False, lengths=None):
-        """``(flags, lens, examined | None, kernel_ms, transfer_ms)`` for a batch."""
+    def run_arrays(self, inputs, with_examined: bool = False, lengths=None, idle=None):
+        """``(flags, lens, examined | None, kernel_ms, transfer_ms)`` for a batch;
+        ``idle`` is called once the launch is enqueued, before the host waits for it."""
         if lengths is None:
             lengths = _lengths(inputs)
         t0 = time.perf_counter()
@@ -113,6 +116,8 @@ class _BatchExecutor:
         r.fetch(n, stream)
         if self.end_to_end:
             e1.record(stream)
+        if idle is not None:
+            idle()
         stream.synchronize()
         kernel_ms = e0.elapsed_time(e1)
         wall_ms = (time.perf_counter() - t0) * 1e3
@@ -124,13 +129,23 @@ class _BatchExecutor:
         return flags, lens, examined, kernel_ms, max(0.0, wall_ms - kernel_ms)
 
     def run_batch(self, inputs) -> list[Result]:
-        if not inputs:
-            return []
-        flags, lens, _, kms, tms = self.run_arrays(inputs)
-        return batch_results(flags, lens, kms, tms)
+        return run_batch_results(self, inputs)
 
     def run(self, input_bytes: bytes) -> Result:
         return self.run_batch([input_bytes])[0]
+
+
+def run_batch_results(executor, inputs, result_cls=Result) -> list:
+    """``executor.run_arrays`` on ``inputs`` as one ``result_cls`` per input, built while
+    the device runs and filled with the verdicts afterwards."""
+    if not inputs:
+        return []
+    out: list = []
+    flags, lens, _, kms, tms = executor.run_arrays(
+        inputs, idle=lambda: out.extend(blank_results(len(inputs), result_cls)))
+    if not out:  # a path that did not call idle
+        out = blank_results(len(inputs), result_cls)
+    return fill_results(out, flags, lens, float(kms), float(tms))
 
 
 class CudaNFAExecutor(_BatchExecutor):
@@ -212,17 +227,14 @@ class CudaPersistentExecutor:
         self.engine = PersistentEngine([automaton], device, choices=[choice],
                                        resident=[resident] if resident is not None else None)
 
-    def run_arrays(self, inputs, with_examined: bool = False, lengths=None):
+    def run_arrays(self, inputs, with_examined: bool = False, lengths=None, idle=None):
         if lengths is None:
             lengths = _lengths(inputs)
         return self.engine.run_requests(np.zeros(len(inputs), dtype=np.int64), inputs,
-                                        with_examined, lengths=lengths)
+                                        with_examined, lengths=lengths, idle=idle)
 
     def run_batch(self, inputs) -> list[Result]:
-        if not inputs:
-            return []
-        flags, lens, _, kms, tms = self.run_arrays(inputs)
-        return batch_results(flags, lens, kms, tms)
+        return run_batch_results(self, inputs)
 
     def run(self, input_bytes: bytes) -> Result:
         return self.run_batch([input_bytes])[0]
@@ -251,19 +263,16 @@ class CudaAutoNFAExecutor:
                                                   resident=self.plain.dev)
         return self._engine
 
-    def run_arrays(self, inputs, with_examined: bool = False):
+    def run_arrays(self, inputs, with_examined: bool = False, idle=None):
         lengths = _lengths(inputs)
         if prefer_engine(self.plain.dev, lengths):
             self.last_path = "engine"
-            return self.engine().run_arrays(inputs, with_examined, lengths)
+            return self.engine().run_arrays(inputs, with_examined, lengths, idle)
         self.last_path = "plain"
-        return self.plain.run_arrays(inputs, with_examined, lengths)
+        return self.plain.run_arrays(inputs, with_examined, lengths, idle)
 
     def run_batch(self, inputs) -> list[Result]:
-        if not inputs:
-            return []
-        flags, lens, _, kms, tms = self.run_arrays(inputs)
-        return batch_results(flags, lens, kms, tms)
+        return run_batch_results(self, inputs)
 
     def run(self, input_bytes: bytes) -> Result:
         return self.run_batch([input_bytes])[0]

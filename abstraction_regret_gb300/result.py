@@ -50,6 +50,31 @@ def batch_results(
     return out
 
 
+def blank_results(n: int, result_cls=Result) -> list:
+    """``n`` results with empty verdicts and zero times, for ``fill_results``: a batch's
+    executor builds them while the device runs, so that only the verdicts are written
+    once the device has finished."""
+    return [result_cls(False, 0) for _ in range(n)]
+
+
+def fill_results(out: list, flags, lens, kernel_ms: float, transfer_ms: float = 0.0) -> list:
+    """Write a batch's verdicts into ``out`` (from ``blank_results``) with the timing
+    convention of ``batch_results``; the objects equal those ``batch_results`` builds."""
+    f = (flags != 0).tolist() if hasattr(flags, "tolist") else [bool(x) for x in flags]
+    m = lens.tolist() if hasattr(lens, "tolist") else [int(x) for x in lens]
+    if len(out) != len(f):
+        raise ValueError(f"{len(out)} results for {len(f)} verdicts")
+    for r, a, b in zip(out, f, m):
+        r.accepted = a
+        r.match_len = b
+    if out:
+        first = out[0]
+        first.kernel_ms = kernel_ms
+        first.total_ms = kernel_ms + transfer_ms
+        first.transfer_ms = transfer_ms
+    return out
+
+
 @dataclass
 class BenchmarkStats:
     """Timings of ``n`` repeated runs after warm-up: mean, sample std, normal CI95."""

@@ -370,3 +370,33 @@ def test_batch_results_values_and_timing_convention():
         assert all(r.kernel_ms == r.total_ms == r.transfer_ms == 0.0 for r in res[1:])
         assert isinstance(res[0], Result)
     assert batch_results([], [], 1.0) == []
+
+
+def test_fill_results_equal_batch_results():
+    """Results built before the verdicts and filled afterwards equal batch_results's."""
+    from abstraction_regret_gb300.executors import run_batch_results
+    from abstraction_regret_gb300.result import batch_results, blank_results, fill_results
+
+    rng = np.random.default_rng(1)
+    flags = rng.integers(0, 2, 50).astype(np.int32)
+    lens = rng.integers(0, 1000, 50).astype(np.int32)
+    for n in (0, 1, 50):
+        got = fill_results(blank_results(n), flags[:n], lens[:n], 3.0, 0.25)
+        assert got == batch_results(flags[:n], lens[:n], 3.0, 0.25)
+        assert got == fill_results(blank_results(n), flags[:n].tolist(), lens[:n].tolist(),
+                                   3.0, 0.25)
+    with pytest.raises(ValueError):
+        fill_results(blank_results(2), flags[:3], lens[:3], 1.0)
+
+    class Stand:
+        calls = 0
+
+        def run_arrays(self, inputs, idle=None):
+            if idle is not None:
+                Stand.calls += 1
+                idle()
+            return flags[:len(inputs)], lens[:len(inputs)], None, 2.0, 1.0
+
+    assert run_batch_results(Stand(), []) == []
+    assert run_batch_results(Stand(), [b"a"] * 7) == batch_results(flags[:7], lens[:7], 2.0, 1.0)
+    assert Stand.calls == 1

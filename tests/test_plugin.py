@@ -92,3 +92,37 @@ def test_reference_objects_run_through_the_engine_when_a_gpu_is_present():
         print("ok")
     """)
     assert out.strip().splitlines()[-1] in ("ok", "skip")
+
+
+def test_adapter_results_equal_gpufsm_batch_results():
+    """The adapter builds gpufsm's own Result objects while the device runs and fills in
+    the verdicts afterwards: they must equal what gpufsm's batch_results builds from the
+    same verdicts and times, field by field (a stand-in executor, no device)."""
+    out = _run("""
+        import numpy as np
+        from gpufsm.core import result as GR
+        import abstraction_regret_gb300.plugin as plugin
+
+        rng = np.random.default_rng(0)
+        flags = rng.integers(0, 2, 300).astype(np.int32)
+        lens = rng.integers(0, 1 << 20, 300).astype(np.int32)
+
+        class Stand:
+            def __init__(self, call_idle):
+                self.call_idle = call_idle
+            def run_arrays(self, inputs, idle=None):
+                if idle is not None and self.call_idle:
+                    idle()
+                n = len(inputs)
+                return flags[:n], lens[:n], None, 1.25, 0.5
+
+        for call_idle in (True, False):
+            for n in (0, 1, 300):
+                got = plugin._Adapter(Stand(call_idle), GR.Result).run_batch([b"x"] * n)
+                want = GR.batch_results(flags[:n], lens[:n], 1.25, 0.5)
+                assert got == want, (call_idle, n)
+                assert all(type(g) is GR.Result for g in got)
+                assert all(type(g.accepted) is bool and type(g.match_len) is int for g in got)
+        print("ok")
+    """)
+    assert out.split()[-1] == "ok"
