@@ -23,7 +23,10 @@ inputs stay larger than L2 where the case's kernel streams them:
 * ``gather``         the batch gather (``gather_inputs_kernel``) of the first 1024
                      c3-sustained inputs as Python ``bytes`` (130 MB, read in place from
                      pageable host memory); the device buffer is checked byte for byte
-                     against the packed batch instead of the oracle.
+                     against the packed batch instead of the oracle;
+* ``run-batch``      the drop-in call ``run_batch(nfa, inputs)`` on c3-sustained with
+                     Python ``bytes`` and the default technique (gather, planning, lanes,
+                     fix-up, verdicts); ``--time`` prints its wall clock per call.
 """
 
 from __future__ import annotations
@@ -52,6 +55,20 @@ def run(case: str, steps: int) -> float | None:
     from .executors import CudaDFAExecutor, CudaNFAExecutor
 
     dev = torch.device("cuda", torch.cuda.current_device())
+    if case == "run-batch":
+        import time
+
+        from .api import run_batch
+
+        b = W.c3("sustained")
+        nfa, inputs = b.automata[0], b.inputs()
+        res = run_batch(nfa, inputs)
+        want = O.nfa_batch(nfa, b.data, b.offsets)[:2]
+        _check(case, ([r.accepted for r in res], [r.match_len for r in res]), want)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            run_batch(nfa, inputs)
+        return (time.perf_counter() - t0) * 1e3 / steps if steps else None
     if case == "gather":
         from .staging import Staging
 
@@ -157,7 +174,8 @@ def run(case: str, steps: int) -> float | None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("case", choices=["c1-live", "c1-plain", "c2-sustained", "c4-sustained",
-                                     "dfa-long", "c5-live", "c3-warps", "gather"])
+                                     "dfa-long", "c5-live", "c3-warps", "gather",
+                                     "run-batch"])
     ap.add_argument("--time", action="store_true",
                     help="also print the mean device time of the timed steps")
     ap.add_argument("--steps", type=int, default=2)
@@ -167,7 +185,8 @@ def main(argv=None) -> int:
         "verdicts equal to the oracle"
     print(f"{args.case}: {checked}; {args.steps} more steps run")
     if args.time and ms is not None:
-        print(f"{args.case}: {ms:.4f} ms per engine step (mean of {args.steps})")
+        what = "call (wall clock)" if args.case == "run-batch" else "engine step"
+        print(f"{args.case}: {ms:.4f} ms per {what} (mean of {args.steps})")
     return 0
 
 
