@@ -16,12 +16,14 @@ namespace {
 
 constexpr int kDfaChunkThreads = 128;  // 4 warps per CTA
 constexpr int kDfaChunkWarps = kDfaChunkThreads / 32;
-// resident CTAs per SM the register allocation is bounded for: 8 gives 64 registers (16
-// spilled bytes) and 4864 resident warps, so a wave holds more, shorter chunks: 64 x 4 MiB
-// on a 4096-state DFA took 22.8 ms against 26.0 ms with no bound (72 registers, 7 CTAs
-// per SM); 0 lifts the bound
+// resident CTAs per SM the register allocation is bounded for (0: no bound, 72 registers,
+// 7 CTAs per SM). 8 gives 64 registers (16 spilled bytes) and 4864 resident warps, so a
+// wave holds more, shorter chunks: 64 x 4 MiB on a 4096-state DFA took 22.8 ms against
+// 26.0 ms, but the serving pool's live trace with every request at once lost 16% of its
+// examined rate (p99 105 against 86-89 ms): its long DFA inputs latch within hundreds of
+// bytes, and every extra chunk walks its set of all states before it sees the latch
 #ifndef GBFSM_DFA_CHUNK_MIN_BLOCKS
-#define GBFSM_DFA_CHUNK_MIN_BLOCKS 8
+#define GBFSM_DFA_CHUNK_MIN_BLOCKS 0
 #endif
 #if GBFSM_DFA_CHUNK_MIN_BLOCKS > 0
 #define GBFSM_DFA_CHUNK_BOUNDS __launch_bounds__(kDfaChunkThreads, GBFSM_DFA_CHUNK_MIN_BLOCKS)
