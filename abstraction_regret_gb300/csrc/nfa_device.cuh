@@ -199,8 +199,8 @@ __device__ __forceinline__ void zero_words(uint64_t *p, int W) {
     for (int w = (int)lane_id(); w < W; w += 32) p[w] = 0ull;
 }
 
-// Dense epsilon closure of V. Round 0 expands every member of V; later rounds expand
-// the members first inserted by the previous round (frontier FA/FB).
+// Dense epsilon closure of V. The first pass expands every member of V; each later pass
+// expands the members first inserted by the pass before (frontier FA/FB).
 template <bool kStaged>
 __device__ __forceinline__ int dense_closure(const Rows &R, int W, uint64_t *V, uint64_t *FA,
                                              uint64_t *FB, uint32_t &info_or) {

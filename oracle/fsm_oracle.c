@@ -1,7 +1,7 @@
 /*
  * fsm_oracle.c -- CPU oracle for the automata-simulation hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle that the CUDA path is compared
  * against; it is never linked into, loaded by or called from the product library or
  * its Python package. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
  * leg load it (through oracle/oracle.py).

@@ -1,6 +1,6 @@
 """CPU oracle for the automata-simulation hot path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker the CUDA engine is compared against. Only ``tests/``,
+This module is the oracle the CUDA engine is compared against. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import it; the
 product package (``abstraction_regret_gb300``) never does, and it has no CPU fallback.
 
